@@ -1,0 +1,85 @@
+// One "pass" = a batched 1-D transform along one axis of a strided array,
+// staged through shared memory: gather a tile of lines (with zero-embedding),
+// run a mixed-radix Stockham FFT of length M in shared memory, scatter the
+// tile (with truncation).  Layout permutations (PFFT's TRANSPOSED_IN/OUT
+// layouts), r2c/c2r Hermitian handling, r2r symmetric extensions, conjugation
+// and the (-1)^k index-shift signs are all folded into the gather/scatter.
+#pragma once
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+namespace pg {
+
+enum ArithId { ARITH_F32 = 0, ARITH_F64 = 1, ARITH_DF = 2 };
+
+// How the logical length-N input line is turned into the length-M complex
+// sequence in shared memory, and how the output line is read back.
+enum PassMode {
+  MODE_C2C = 0,   // complex in, complex out, M == N
+  MODE_R2C = 1,   // real in, complex out (bins 0..N/2), M == N
+  MODE_C2R = 2,   // complex half spectrum in, real out, M == N
+  MODE_RE00 = 3,  // FFTW_REDFT00, M = 2(N-1)
+  MODE_RE01 = 4,  // FFTW_REDFT01, M = 4N
+  MODE_RE10 = 5,  // FFTW_REDFT10, M = 4N
+  MODE_RE11 = 6,  // FFTW_REDFT11, M = 8N
+  MODE_RO00 = 7,  // FFTW_RODFT00, M = 2(N+1)
+  MODE_RO01 = 8,  // FFTW_RODFT01, M = 4N
+  MODE_RO10 = 9,  // FFTW_RODFT10, M = 4N
+  MODE_RO11 = 10, // FFTW_RODFT11, M = 8N
+  MODE_R2HC = 11, // FFTW_R2HC, M = N
+  MODE_HC2R = 12, // FFTW_HC2R, M = N (backward)
+  MODE_DHT = 13,  // FFTW_DHT, M = N
+  MODE_COPYR = 14 // real identity (skipped r2r axis), M = N
+};
+
+// (-1)^k sign pattern of PFFT's SHIFTED flags along one axis:
+// factor(i) = (en && i+start < thresh) ? ((i+start odd) ? -extra : extra) : 1
+struct ShiftSign {
+  int en;
+  int start;
+  int thresh;
+  int extra;
+};
+
+#define PG_MAX_BATCH 8
+#define PG_MAX_STAGES 24
+
+struct PassParams {
+  const void* src;
+  void* dst;
+  const void* tw;      // twiddle table W_M^m, m < M, in the policy's sm_t format
+  int mode;
+  int sign;            // -1 forward, +1 backward (the complex FFT direction)
+  int N;               // logical transform length along the axis
+  int M;               // complex FFT length run in shared memory
+  int Ni, Zi;          // input count and its offset in the logical sequence
+  int No, Zo;          // output count and the logical offset it starts at
+  long long sIa, sOa;  // element strides along the axis (input / output)
+  int nb;              // batch dims (fastest first)
+  long long bext[PG_MAX_BATCH];
+  long long bsI[PG_MAX_BATCH];
+  long long bsO[PG_MAX_BATCH];
+  ShiftSign bshI[PG_MAX_BATCH];  // per batch dim sign (load side)
+  ShiftSign bshO[PG_MAX_BATCH];  // per batch dim sign (store side)
+  ShiftSign ashI, ashO;          // axis sign (load / store side)
+  long long nlines;
+  int L;        // lines per CTA
+  int LS;       // shared-memory line stride (elements)
+  int nst;      // number of stages
+  int radix[PG_MAX_STAGES];
+  int pingpong; // 1 if a generic (large prime) stage needs a second buffer
+  int conj_in, conj_out;
+  int wmode;    // adjoint weights: 1 = halve interior half-spectrum bins on load
+                // (C2R), 2 = double interior bins on store (R2C)
+  int in_contig, out_contig;  // axis has unit stride on that side
+  int threads;
+  int smem_bytes;
+};
+
+// Launch one pass on `stream`.  Returns a cudaError_t value.
+int launch_pass(const PassParams& p, int arith, cudaStream_t stream);
+
+// Shared-memory element size of a policy.
+inline int arith_sm_bytes(int arith) { return arith == ARITH_F32 ? 8 : 16; }
+
+}  // namespace pg

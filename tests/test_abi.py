@@ -1,0 +1,38 @@
+"""The C-ABI library loads and exports every entry point its headers declare
+(no GPU needed)."""
+import os
+import re
+import subprocess
+
+import pfft_gb300 as pg
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    syms = set()
+    hdr = open(os.path.join(ROOT, "include", "pfft.h")).read()
+    body = hdr[hdr.index("#define PFFT_GB300_DECLARE"):hdr.index("PFFT_GB300_DECLARE(pfft_, double")]
+    names = set(re.findall(r"PX##(\w+)\s*\(", body))
+    for pre in ("pfft_", "pfftf_"):
+        syms |= {pre + nm for nm in names}
+    for h in ("pfft_gb300.h", "mpi.h"):
+        txt = open(os.path.join(ROOT, "include", h)).read()
+        txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+        for m in re.finditer(r"^[A-Za-z_][\w \*]*?\b((?:pfftf?_|MPI_)\w+)\s*\(", txt, flags=re.M):
+            syms.add(m.group(1))
+    return syms
+
+
+def test_library_exports_all_declared_symbols(pfft_lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", pg.LIBPATH], capture_output=True, text=True).stdout
+    exported = {ln.split()[-1] for ln in out.splitlines() if ln.strip()}
+    want = declared_symbols()
+    assert len(want) > 250
+    missing = sorted(want - exported)
+    assert not missing, missing
+
+
+def test_library_has_no_torch_dependency(pfft_lib):
+    out = subprocess.run(["ldd", pg.LIBPATH], capture_output=True, text=True).stdout
+    assert "torch" not in out and "c10" not in out

@@ -1,0 +1,142 @@
+"""GPU parity of pfft_execute against the CPU oracle, through the C-ABI.
+
+Cases follow the reference's check programs (tests/simple_check_*.c): their
+sizes (29x27x31, 13x14x19x17, 2x2x4, 16^3 <-> 29x27x31 oversampling),
+transposed layouts, in-place and out-of-place arrays, r2c/c2r padding, the
+r2r kinds they use, plus the configurations of the benchmark suite at sizes
+the oracle finishes in seconds.  Tolerances: relative L2 <= 1e-12 for the
+double API, <= 2e-6 for the float API.
+"""
+import numpy as np
+import pytest
+
+import pfft_gb300 as pg
+from tests.pfft_util import Req, gpu_run, oracle_run, random_input, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"double": 1e-12, "float": 2e-6}
+TO, TI = pg.PFFT_TRANSPOSED_OUT, pg.PFFT_TRANSPOSED_IN
+PAD = pg.PFFT_PADDED_R2C
+
+
+def check(req, prec="double", inplace=False, dist="uniform", seed=1):
+    rng = np.random.default_rng(seed)
+    x = random_input(req, rng, dist)
+    if prec == "float":
+        x = x.astype(np.float32).astype(np.float64)
+    ref = oracle_run(req, x)
+    got = gpu_run(req, x, prec=prec, inplace=inplace)
+    err = rel_l2(got, ref)
+    assert err <= TOL[prec], "rel L2 %.3e > %.1e" % (err, TOL[prec])
+    return err
+
+
+C2C_CASES = [
+    ((8, 8, 8), 0), ((2, 2, 4), 0), ((29, 27, 31), 0), ((64, 64, 64), 0), ((29, 27, 31), TO),
+    ((29, 27, 31), TI), ((64, 64, 64), TO), ((16, 12, 10), TI), ((5, 7, 11), 0), ((48, 64, 40), 0),
+    ((96, 32, 17), 0),
+]
+
+
+@pytest.mark.parametrize("n,flags", C2C_CASES)
+@pytest.mark.parametrize("prec", ["double", "float"])
+def test_c2c_3d(cuda, pfft_lib, n, flags, prec):
+    check(Req("c2c", n, flags=flags), prec)
+
+
+@pytest.mark.parametrize("sign", [-1, 1])
+def test_c2c_backward_and_inplace(cuda, pfft_lib, sign):
+    check(Req("c2c", (29, 27, 31), sign=sign), inplace=True)
+    check(Req("c2c", (29, 27, 31), sign=sign, flags=TO), inplace=True)
+
+
+@pytest.mark.parametrize("n,flags", [((8, 8, 8), 0), ((29, 27, 31), 0), ((16, 16, 16), TO), ((29, 27, 31), TO),
+                                     ((16, 16, 16), PAD), ((29, 27, 31), PAD | TO), ((64, 64, 64), PAD | TO)])
+@pytest.mark.parametrize("prec", ["double", "float"])
+def test_r2c(cuda, pfft_lib, n, flags, prec):
+    check(Req("r2c", n, flags=flags), prec, dist="normal")
+
+
+@pytest.mark.parametrize("n,flags", [((8, 8, 8), 0), ((29, 27, 31), 0), ((16, 16, 16), TI), ((29, 27, 31), TI),
+                                     ((16, 16, 16), PAD), ((29, 27, 31), PAD | TI), ((64, 64, 64), PAD | TI)])
+@pytest.mark.parametrize("prec", ["double", "float"])
+def test_c2r(cuda, pfft_lib, n, flags, prec):
+    check(Req("c2r", n, sign=1, flags=flags), prec)
+
+
+def test_r2c_backward_c2r_forward(cuda, pfft_lib):
+    # conjugation paths (kernel/partrafo.c:428-443)
+    check(Req("r2c", (12, 10, 16), sign=1), dist="normal")
+    check(Req("c2r", (12, 10, 16), sign=-1))
+
+
+def test_r2c_c2r_inplace_padded(cuda, pfft_lib):
+    check(Req("r2c", (16, 12, 10), flags=PAD), inplace=True, dist="normal")
+    check(Req("c2r", (16, 12, 10), sign=1, flags=PAD), inplace=True)
+    check(Req("r2c", (16, 12, 10), flags=PAD | TO), inplace=True, dist="normal")
+    check(Req("c2r", (16, 12, 10), sign=1, flags=PAD | TI), inplace=True)
+
+
+@pytest.mark.parametrize("kinds", [(3, 3, 3), (4, 4, 4), (5, 5, 5), (6, 6, 6), (7, 7, 7), (8, 8, 8), (9, 9, 9),
+                                   (10, 10, 10), (0, 1, 2), (3, 4, 7), (5, 9, 6)])
+@pytest.mark.parametrize("prec", ["double", "float"])
+def test_r2r(cuda, pfft_lib, kinds, prec):
+    check(Req("r2r", (9, 8, 10), kinds=list(kinds)), prec, dist="normal")
+
+
+def test_r2r_transposed(cuda, pfft_lib):
+    check(Req("r2r", (16, 16, 16), kinds=[5, 5, 5], flags=TO), dist="normal")
+    check(Req("r2r", (16, 16, 16), kinds=[4, 4, 4], flags=TI), dist="normal")
+
+
+def test_ousam_c2c(cuda, pfft_lib):
+    # tests/simple_check_ousam_c2c.c: ni = 16^3 -> n = 29x27x31 -> no = n, and back
+    check(Req("c2c", (29, 27, 31), ni=(16, 16, 16)))
+    check(Req("c2c", (29, 27, 31), no=(16, 16, 16), sign=1))
+    check(Req("c2c", (29, 27, 31), ni=(16, 16, 16), no=(20, 18, 16), flags=TO))
+
+
+def test_ousam_r2c_c2r(cuda, pfft_lib):
+    check(Req("r2c", (29, 27, 31), ni=(16, 16, 16)), dist="normal")
+    check(Req("c2r", (29, 27, 31), no=(16, 16, 16), sign=1))
+    check(Req("r2c", (32, 32, 32), ni=(16, 16, 16), flags=PAD | TO), dist="normal")
+    # truncated r2c output keeps the reference's bin range
+    check(Req("r2c", (32, 30, 28), no=(16, 16, 16)), dist="normal")
+
+
+def test_shifted(cuda, pfft_lib):
+    S_IN, S_OUT = pg.PFFT_SHIFTED_IN, pg.PFFT_SHIFTED_OUT
+    check(Req("c2c", (8, 10, 12), flags=S_IN | S_OUT))
+    check(Req("c2c", (8, 10, 12), flags=S_OUT))
+    check(Req("c2c", (8, 10, 12), flags=S_IN))
+    check(Req("c2c", (16, 16, 16), ni=(8, 8, 8), flags=S_IN | S_OUT))
+    check(Req("r2c", (8, 10, 12), flags=S_IN | S_OUT), dist="normal")
+
+
+def test_4d_and_meshes(cuda, pfft_lib):
+    check(Req("c2c", (13, 14, 19, 17)))
+    check(Req("c2c", (13, 14, 19, 17), flags=TO))
+    check(Req("c2c", (8, 6, 10, 4), cart=3))
+    check(Req("c2c", (8, 6, 10, 4), cart=3, flags=TO))
+    check(Req("c2c", (12, 10, 8), cart=1, flags=TO))
+    check(Req("c2c", (12, 10, 8), cart=0, flags=TO))
+    check(Req("c2c", (12, 10, 8), cart=3, flags=TO))
+    check(Req("r2c", (12, 10, 8), cart=3, flags=PAD), dist="normal")
+
+
+def test_howmany(cuda, pfft_lib):
+    check(Req("c2c", (8, 8, 8), howmany=2))
+    check(Req("c2c", (8, 8, 8), howmany=3, flags=TO))
+    check(Req("r2c", (8, 8, 8), howmany=2), dist="normal")
+    check(Req("c2r", (8, 8, 8), howmany=2, sign=1))
+
+
+def test_native_f64_arith(cuda, pfft_lib):
+    L = pg.lib()
+    L.pfft_gb300_set_double_arith(1)
+    try:
+        check(Req("c2c", (29, 27, 31), flags=TO))
+        check(Req("r2c", (16, 16, 16), flags=PAD), dist="normal")
+    finally:
+        L.pfft_gb300_set_double_arith(0)
