@@ -49,6 +49,15 @@ int pfft_gb300_pass_info(const pfft_plan plan, int i, int *axis, int *M, int *L,
 int pfftf_gb300_pass_info(const pfftf_plan plan, int i, int *axis, int *M, int *L, int *threads, int *smem,
                           double *bytes);
 
+/* Per-pass timing with CUDA events recorded on the plan's stream around every
+ * pass launch of pfft_execute (also feeds the plan timer's stage slots).
+ * pass_time returns the accumulated milliseconds of pass i and the number of
+ * timed executions. */
+int pfft_gb300_set_pass_timing(pfft_plan plan, int on);
+int pfftf_gb300_set_pass_timing(pfftf_plan plan, int on);
+int pfft_gb300_pass_time(const pfft_plan plan, int i, double *ms_total, int *runs);
+int pfftf_gb300_pass_time(const pfftf_plan plan, int i, double *ms_total, int *runs);
+
 /* Arithmetic of the double API: 0 = float-float on the FP32 pipes (default),
  * 1 = native FP64.  Applies to plans created afterwards. */
 void pfft_gb300_set_double_arith(int mode);

@@ -157,6 +157,10 @@ def _declare(L):
         f("gb300_plan_info").restype = ctypes.c_int
         f("gb300_plan_info").argtypes = [c_void_p, _IP, ctypes.POINTER(ctypes.c_double),
                                          ctypes.POINTER(ctypes.c_size_t)]
+        f("gb300_set_pass_timing").restype = ctypes.c_int
+        f("gb300_set_pass_timing").argtypes = [c_void_p, ctypes.c_int]
+        f("gb300_pass_time").restype = ctypes.c_int
+        f("gb300_pass_time").argtypes = [c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double), _IP]
         f("gb300_pass_info").restype = ctypes.c_int
         f("gb300_pass_info").argtypes = [c_void_p, ctypes.c_int, _IP, _IP, _IP, _IP, _IP,
                                          ctypes.POINTER(ctypes.c_double)]

@@ -379,7 +379,19 @@ void do_execute(Plan* pl, void* in, void* out) {
     if (bytes) *bytes = ps.bytes;                                                                         \
     return 0;                                                                                             \
   }                                                                                                       \
-  void* PX##gb300_internal(const PX##plan plan) { return plan ? (void*)plan->p : nullptr; }               \
+  int PX##gb300_set_pass_timing(PX##plan plan, int on) {                                                 \
+    if (!plan) return -1;                                                                                 \
+    plan->p->time_passes = on != 0;                                                                       \
+    plan->p->pass_ms.assign(plan->p->fwd.passes.size(), 0.0);                                             \
+    plan->p->timed_runs = 0;                                                                              \
+    return 0;                                                                                             \
+  }                                                                                                       \
+  int PX##gb300_pass_time(const PX##plan plan, int i, double* ms_total, int* runs) {                      \
+    if (!plan || i < 0 || i >= (int)plan->p->pass_ms.size()) return -1;                                   \
+    if (ms_total) *ms_total = plan->p->pass_ms[i];                                                        \
+    if (runs) *runs = plan->p->timed_runs;                                                                \
+    return 0;                                                                                             \
+  }                                                                                                       \
   }
 
 PG_API(pfft_, 1, double, pfft_complex)

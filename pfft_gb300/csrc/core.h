@@ -159,6 +159,11 @@ struct Plan {
   int graph_dir = 0;
   TimerData timer;
   cudaEvent_t ev[2] = {nullptr, nullptr};
+  // optional per-pass timing with CUDA events on the plan stream
+  bool time_passes = false;
+  std::vector<cudaEvent_t> pev;
+  std::vector<double> pass_ms;
+  int timed_runs = 0;
 };
 
 // Build the pass program of a plan (planner.cpp).  Returns false on failure

@@ -81,7 +81,18 @@ bool ensure_workspace(Plan* pl, const PassProgram& prog) {
 
 int run_program(Plan* pl, const PassProgram& prog, void* in, void* out, cudaStream_t s) {
   void* bufs[4] = {in, out, pl->ws[0], pl->ws[1]};
-  for (const Pass& ps : prog.passes) {
+  const bool timing = pl->time_passes && &prog == &pl->fwd;
+  const size_t np = prog.passes.size();
+  if (timing && pl->pev.size() < np + 1) {
+    for (auto e : pl->pev) cudaEventDestroy(e);
+    pl->pev.assign(np + 1, nullptr);
+    for (auto& e : pl->pev)
+      if (cudaEventCreate(&e) != cudaSuccess) return (int)cudaGetLastError();
+    pl->pass_ms.assign(np, 0.0);
+  }
+  if (timing) cudaEventRecord(pl->pev[0], s);
+  for (size_t i = 0; i < np; i++) {
+    const Pass& ps = prog.passes[i];
     PassParams p = ps.p;
     p.src = bufs[ps.src];
     p.dst = bufs[ps.dst];
@@ -90,8 +101,22 @@ int run_program(Plan* pl, const PassProgram& prog, void* in, void* out, cudaStre
     if (!p.tw) return (int)e;
     int rc = launch_pass(p, pl->arith, s);
     if (rc) return rc;
+    if (timing) cudaEventRecord(pl->pev[i + 1], s);
   }
   return 0;
+}
+
+// accumulate the per-pass event times of the last run (after a synchronize)
+static void collect_pass_times(Plan* pl) {
+  if (!pl->time_passes || pl->pev.empty()) return;
+  for (size_t i = 0; i + 1 < pl->pev.size() && i < pl->pass_ms.size(); i++) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, pl->pev[i], pl->pev[i + 1]) == cudaSuccess) {
+      pl->pass_ms[i] += ms;
+      if (i < pl->timer.trafo.size()) pl->timer.trafo[i] += 1e-3 * ms;
+    }
+  }
+  pl->timed_runs++;
 }
 
 Plan* make_plan(const PlanDesc& base, void* in, void* out) {
@@ -133,6 +158,7 @@ void destroy_plan(Plan* pl) {
   if (pl->graph) cudaGraphExecDestroy(pl->graph);
   for (int k = 0; k < 2; k++)
     if (pl->ev[k]) cudaEventDestroy(pl->ev[k]);
+  for (auto e : pl->pev) cudaEventDestroy(e);
   delete pl;
 }
 
@@ -237,6 +263,7 @@ void execute_plan(Plan* pl, void* in, void* out, bool adjoint) {
     if (cuda_check(cudaStreamSynchronize(s), "execute")) return;
     auto t1 = std::chrono::steady_clock::now();
     pl->timer.whole += std::chrono::duration<double>(t1 - t0).count();
+    if (!adjoint && !(pl->use_graph && din && dout)) collect_pass_times(pl);
   }
   pl->timer.iter++;
 }

@@ -126,6 +126,17 @@ def gpu_run(req, x, prec="double", inplace=False, adjoint=False, torch=None, kee
     return out
 
 
+def mask_padding(req, out):
+    """Zero the row padding of a padded c2r output (its contents are
+    unspecified, as in the reference, which uses the output as scratch)."""
+    if req.kind != "c2r" or not req.padded():
+        return out
+    _, _, _, lno, _ = req.sizes()
+    a = np.array(out, dtype=np.float64).reshape(-1, lno[-1] * req.howmany)
+    a[:, req.no[-1] * req.howmany:] = 0
+    return a.ravel()
+
+
 def rel_l2(a, b):
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
