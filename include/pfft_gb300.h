@@ -63,6 +63,12 @@ int pfftf_gb300_pass_time(const pfftf_plan plan, int i, double *ms_total, int *r
 void pfft_gb300_set_double_arith(int mode);
 int pfft_gb300_get_double_arith(void);
 
+/* Kernel selection: 1 (default) runs power-of-two c2c passes on the
+ * register-resident radix-8 kernel, 0 uses the general pass kernel everywhere
+ * (also set by the environment variable PFFT_GB300_KERNEL=generic). */
+void pfft_gb300_set_kernel_path(int path);
+int pfft_gb300_get_kernel_path(void);
+
 /* Last error (CUDA error code or library error) and its message. */
 int pfft_gb300_last_error(void);
 const char *pfft_gb300_last_error_string(void);

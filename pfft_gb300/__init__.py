@@ -167,6 +167,8 @@ def _declare(L):
     L.pfft_gb300_last_error.restype = ctypes.c_int
     L.pfft_gb300_last_error_string.restype = ctypes.c_char_p
     L.pfft_gb300_set_double_arith.argtypes = [ctypes.c_int]
+    L.pfft_gb300_set_kernel_path.argtypes = [ctypes.c_int]
+    L.pfft_gb300_get_kernel_path.restype = ctypes.c_int
     L.pfft_gb300_get_double_arith.restype = ctypes.c_int
 
 

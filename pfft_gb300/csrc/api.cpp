@@ -401,6 +401,8 @@ extern "C" {
 int pfft_gb300_last_error(void) { return last_error_code(); }
 const char* pfft_gb300_last_error_string(void) { return last_error_string(); }
 void pfft_gb300_clear_error(void) { clear_error(); }
+void pfft_gb300_set_kernel_path(int path) { set_kernel_path(path ? 1 : 0); }
+int pfft_gb300_get_kernel_path(void) { return kernel_path(); }
 void pfft_gb300_set_double_arith(int mode) { set_double_arith(mode == 1 ? ARITH_F64 : ARITH_DF); }
 int pfft_gb300_get_double_arith(void) { return double_arith() == ARITH_F64 ? 1 : 0; }
 }

@@ -6,6 +6,8 @@
 // so after the last stage the line is in natural order.  Radices 2,3,4,5,8,16
 // have dedicated butterflies, small odd primes (7, 11, 13) use a register DFT
 // with table twiddles, and any other prime uses a shared-memory ping-pong stage.
+#include <stdlib.h>
+#include <string.h>
 #include "pass.h"
 #include "arith.cuh"
 
@@ -504,7 +506,23 @@ static int launch_t(const PassParams& p, cudaStream_t stream) {
   return (int)cudaGetLastError();
 }
 
+int launch_fast_pass(const PassParams& p, int arith, cudaStream_t stream);
+
+static int g_kernel_path = -1;  // 0 generic only, 1 fast kernel where it applies
+int kernel_path() {
+  if (g_kernel_path < 0) {
+    const char* e = getenv("PFFT_GB300_KERNEL");
+    g_kernel_path = (e && strcmp(e, "generic") == 0) ? 0 : 1;
+  }
+  return g_kernel_path;
+}
+void set_kernel_path(int v) { g_kernel_path = v; }
+
 int launch_pass(const PassParams& p, int arith, cudaStream_t stream) {
+  if (kernel_path() == 1) {
+    int rc = launch_fast_pass(p, arith, stream);
+    if (rc != -1) return rc;
+  }
   switch (arith) {
     case ARITH_F32: return launch_t<ArF32>(p, stream);
     case ARITH_F64: return launch_t<ArF64>(p, stream);

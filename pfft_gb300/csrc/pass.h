@@ -78,6 +78,9 @@ struct PassParams {
 
 // Launch one pass on `stream`.  Returns a cudaError_t value.
 int launch_pass(const PassParams& p, int arith, cudaStream_t stream);
+// 1: use the register-resident kernel where it applies (default), 0: generic only
+int kernel_path();
+void set_kernel_path(int v);
 
 // Shared-memory element size of a policy.
 inline int arith_sm_bytes(int arith) { return arith == ARITH_F32 ? 8 : 16; }

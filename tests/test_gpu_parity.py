@@ -140,3 +140,20 @@ def test_native_f64_arith(cuda, pfft_lib):
         check(Req("r2c", (16, 16, 16), flags=PAD), dist="normal")
     finally:
         L.pfft_gb300_set_double_arith(0)
+
+
+@pytest.mark.parametrize("n,flags", [((64, 64, 64), 0), ((128, 64, 256), TO), ((512, 8, 16), 0),
+                                     ((16, 1024, 8), TI), ((2048, 4, 4), 0), ((8, 4, 4096), 0)])
+@pytest.mark.parametrize("prec", ["double", "float"])
+def test_kernel_paths_agree(cuda, pfft_lib, n, flags, prec):
+    """The register-resident radix-8 kernel and the general pass kernel both
+    match the oracle on power-of-two c2c lines (row, column and transposing
+    passes, every supported line length)."""
+    L = pg.lib()
+    try:
+        for path in (1, 0):
+            L.pfft_gb300_set_kernel_path(path)
+            check(Req("c2c", n, flags=flags), prec)
+            check(Req("c2c", n, flags=flags, sign=1), prec)
+    finally:
+        L.pfft_gb300_set_kernel_path(1)
