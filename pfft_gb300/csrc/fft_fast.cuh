@@ -1,0 +1,370 @@
+// Register-resident radix-8 pass for power-of-two c2c lines (64..4096).
+//
+// The generic pass (fft_pass.cu) stages every stage through shared memory and
+// handles every mode.  This kernel covers the hot case - a plain c2c line
+// transform with no embedding, truncation or index-shift signs - with:
+//   * each thread owning one radix-8 butterfly per stage (N/8 threads a line),
+//     eight complex values held in registers;
+//   * stage 1 loading straight from global memory and the last stage storing
+//     straight to global memory, both coalesced (consecutive threads walk the
+//     contiguous direction: along the line for rows, across lines for
+//     columns); only the stages in between exchange through shared memory,
+//     double-buffered so each stage needs one barrier;
+//   * a padded shared-memory index p + p/8 that keeps the stride-8 Stockham
+//     writes free of bank conflicts;
+//   * for the double API, float-float arithmetic with unnormalised additions
+//     (TwoSum on the high parts, plain sums of the low parts) renormalised
+//     once per butterfly output.
+// A length N = 8^a * q (q = 1, 2, 4) runs a radix-8 stages and one radix-q stage.
+#pragma once
+#include "arith.cuh"
+#include "pass.h"
+
+namespace pg {
+
+namespace fast {
+
+// ---- arithmetic -----------------------------------------------------------------
+struct F32 {
+  typedef float2 S;   // shared / twiddle element
+  typedef float2 G;   // global element
+  typedef float2 C;
+  static __device__ __forceinline__ C add(C a, C b) { return make_float2(a.x + b.x, a.y + b.y); }
+  static __device__ __forceinline__ C sub(C a, C b) { return make_float2(a.x - b.x, a.y - b.y); }
+  static __device__ __forceinline__ C mul(C a, S w) {
+    return make_float2(__fmaf_rn(a.x, w.x, -a.y * w.y), __fmaf_rn(a.x, w.y, a.y * w.x));
+  }
+  static __device__ __forceinline__ C scal(C a, float c) { return make_float2(a.x * c, a.y * c); }
+  static __device__ __forceinline__ C neg(C a) { return make_float2(-a.x, -a.y); }
+  static __device__ __forceinline__ C swap_neg_re(C a) { return make_float2(-a.y, a.x); }  // *i
+  static __device__ __forceinline__ C swap_neg_im(C a) { return make_float2(a.y, -a.x); }  // *(-i)
+  static __device__ __forceinline__ C renorm(C a) { return a; }
+  static __device__ __forceinline__ C ld(const G* p) { return *p; }
+  static __device__ __forceinline__ void st(G* p, C v) { *p = v; }
+  static __device__ __forceinline__ C lds(const S& s) { return s; }
+  static __device__ __forceinline__ S sts(C v) { return v; }
+  static __device__ __forceinline__ S twc(S w, int sign) { return sign < 0 ? w : make_float2(w.x, -w.y); }
+  static __device__ __forceinline__ C conj(C a) { return make_float2(a.x, -a.y); }
+  static __device__ __forceinline__ float c8() { return 0.70710678118654752440f; }
+};
+
+// lazily-normalised float-float
+struct DD {
+  float hi, lo;
+};
+__device__ __forceinline__ DD dd_add(DD a, DD b) {
+  float s = __fadd_rn(a.hi, b.hi);
+  float bb = __fsub_rn(s, a.hi);
+  float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+  return {s, __fadd_rn(__fadd_rn(a.lo, b.lo), e)};
+}
+__device__ __forceinline__ DD dd_neg(DD a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ DD dd_sub(DD a, DD b) { return dd_add(a, dd_neg(b)); }
+__device__ __forceinline__ DD dd_norm(DD a) {
+  float s = __fadd_rn(a.hi, a.lo);
+  return {s, __fsub_rn(a.lo, __fsub_rn(s, a.hi))};
+}
+// a * c with c a normalised constant
+__device__ __forceinline__ DD dd_mulc(DD a, DD c) {
+  float p = __fmul_rn(a.hi, c.hi);
+  float e = __fmaf_rn(a.hi, c.hi, -p);
+  e = __fmaf_rn(a.hi, c.lo, e);
+  e = __fmaf_rn(a.lo, c.hi, e);
+  return {p, e};
+}
+// a*b - c*d (b, d normalised)
+__device__ __forceinline__ DD dd_mms(DD a, DD b, DD c, DD d) {
+  float p1 = __fmul_rn(a.hi, b.hi);
+  float e1 = __fmaf_rn(a.hi, b.hi, -p1);
+  float p2 = __fmul_rn(c.hi, d.hi);
+  float e2 = __fmaf_rn(c.hi, d.hi, -p2);
+  float s = __fsub_rn(p1, p2);
+  float bb = __fsub_rn(s, p1);
+  float e = __fsub_rn(__fsub_rn(p1, __fsub_rn(s, bb)), __fadd_rn(p2, bb));
+  e = __fadd_rn(e, __fsub_rn(e1, e2));
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  e = __fmaf_rn(-c.hi, d.lo, e);
+  e = __fmaf_rn(-c.lo, d.hi, e);
+  return {s, e};
+}
+
+struct FDD {
+  typedef float4 S;   // (re.hi, re.lo, im.hi, im.lo)
+  typedef double2 G;
+  struct C {
+    DD x, y;
+  };
+  static __device__ __forceinline__ C add(C a, C b) { return {dd_add(a.x, b.x), dd_add(a.y, b.y)}; }
+  static __device__ __forceinline__ C sub(C a, C b) { return {dd_sub(a.x, b.x), dd_sub(a.y, b.y)}; }
+  static __device__ __forceinline__ C mul(C a, S w) {
+    DD wr = {w.x, w.y}, wi = {w.z, w.w};
+    return {dd_mms(a.x, wr, a.y, wi), dd_mms(a.x, wi, dd_neg(a.y), wr)};
+  }
+  static __device__ __forceinline__ C scal(C a, DD c) { return {dd_mulc(a.x, c), dd_mulc(a.y, c)}; }
+  static __device__ __forceinline__ C neg(C a) { return {dd_neg(a.x), dd_neg(a.y)}; }
+  static __device__ __forceinline__ C swap_neg_re(C a) { return {dd_neg(a.y), a.x}; }
+  static __device__ __forceinline__ C swap_neg_im(C a) { return {a.y, dd_neg(a.x)}; }
+  static __device__ __forceinline__ C renorm(C a) { return {dd_norm(a.x), dd_norm(a.y)}; }
+  static __device__ __forceinline__ C ld(const G* p) {
+    G v = *p;
+    df a = df_from_double(v.x), b = df_from_double(v.y);
+    return {{a.hi, a.lo}, {b.hi, b.lo}};
+  }
+  static __device__ __forceinline__ void st(G* p, C v) {
+    *p = make_double2(df_to_double(df{v.x.hi, v.x.lo}), df_to_double(df{v.y.hi, v.y.lo}));
+  }
+  static __device__ __forceinline__ C lds(const S& s) { return {{s.x, s.y}, {s.z, s.w}}; }
+  static __device__ __forceinline__ S sts(C v) { return make_float4(v.x.hi, v.x.lo, v.y.hi, v.y.lo); }
+  static __device__ __forceinline__ S twc(S w, int sign) { return sign < 0 ? w : make_float4(w.x, w.y, -w.z, -w.w); }
+  static __device__ __forceinline__ C conj(C a) { return {a.x, dd_neg(a.y)}; }
+  static __device__ __forceinline__ DD c8() {
+    return {(float)0.70710678118654752440, (float)(0.70710678118654752440 - (double)(float)0.70710678118654752440)};
+  }
+};
+
+// multiply by SIGN*i
+template <class P, int SIGN>
+__device__ __forceinline__ typename P::C msi(typename P::C a) {
+  return SIGN < 0 ? P::swap_neg_im(a) : P::swap_neg_re(a);
+}
+
+template <class P, int SIGN>
+__device__ __forceinline__ void bf4(typename P::C& a0, typename P::C& a1, typename P::C& a2, typename P::C& a3) {
+  typedef typename P::C C;
+  C t0 = P::add(a0, a2), t1 = P::sub(a0, a2);
+  C t2 = P::add(a1, a3), t3 = msi<P, SIGN>(P::sub(a1, a3));
+  a0 = P::add(t0, t2);
+  a2 = P::sub(t0, t2);
+  a1 = P::add(t1, t3);
+  a3 = P::sub(t1, t3);
+}
+
+// in-place radix-8 DFT, natural order in and out
+template <class P, int SIGN>
+__device__ __forceinline__ void bf8(typename P::C* v) {
+  typedef typename P::C C;
+  bf4<P, SIGN>(v[0], v[2], v[4], v[6]);
+  bf4<P, SIGN>(v[1], v[3], v[5], v[7]);
+  const auto c = P::c8();
+  // W8^1 z = c (z + S i z);  W8^3 z = c (S i z - z)
+  C o1 = P::scal(P::add(v[3], msi<P, SIGN>(v[3])), c);
+  C o3 = P::scal(P::sub(msi<P, SIGN>(v[7]), v[7]), c);
+  C o2 = msi<P, SIGN>(v[5]);
+  C e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6], o0 = v[1];
+  v[0] = P::add(e0, o0);
+  v[4] = P::sub(e0, o0);
+  v[1] = P::add(e1, o1);
+  v[5] = P::sub(e1, o1);
+  v[2] = P::add(e2, o2);
+  v[6] = P::sub(e2, o2);
+  v[3] = P::add(e3, o3);
+  v[7] = P::sub(e3, o3);
+}
+
+__device__ __forceinline__ int pad(int p) { return p + (p >> 3); }
+
+__host__ __device__ constexpr int n8_of(int N) { return N >= 4096 ? 4 : (N >= 512 ? 3 : 2); }
+__host__ __device__ constexpr int pow8(int a) { return a == 4 ? 4096 : (a == 3 ? 512 : 64); }
+
+struct FastArgs {
+  const void* src;
+  void* dst;
+  const void* tw;
+  long long sIa, sOa;
+  int nb;
+  long long bext[PG_MAX_BATCH];
+  long long bsI[PG_MAX_BATCH];
+  long long bsO[PG_MAX_BATCH];
+  long long nlines;
+  int conj_in, conj_out;
+};
+
+// ROW_IN: the axis is contiguous on the input side (thread t walks the line);
+// otherwise consecutive threads take consecutive lines.  ROW_OUT likewise for
+// the output; when they differ the last stage goes through shared memory.
+template <class P, int SIGN, int N, int L, bool ROW_IN, bool ROW_OUT>
+__global__ void __launch_bounds__(L*(N / 8)) k_fast(const FastArgs a) {
+  typedef typename P::C C;
+  typedef typename P::S S;
+  typedef typename P::G G;
+  constexpr int TPL = N / 8;  // threads per line
+  constexpr int NS8 = n8_of(N);
+  constexpr int Q = N / pow8(NS8);  // last radix: 1, 2 or 4
+  constexpr int LSP = N + N / 8;    // padded line stride in shared memory
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  long long* offI = (long long*)sm_raw;
+  long long* offO = offI + L;
+  S* buf0 = (S*)(sm_raw + 16 * L);
+  S* buf1 = buf0 + L * LSP;
+
+  const int tid = threadIdx.x;
+  const long long g0 = (long long)blockIdx.x * L;
+  if (tid < L) {
+    long long g = g0 + tid;
+    if (g >= a.nlines) g = a.nlines - 1;  // tail CTA: clamp (duplicate work, same values)
+    long long oi = 0, oo = 0;
+    for (int b = 0; b < a.nb; b++) {
+      long long e = a.bext[b];
+      long long idx = g % e;
+      g /= e;
+      oi += idx * a.bsI[b];
+      oo += idx * a.bsO[b];
+    }
+    offI[tid] = oi;
+    offO[tid] = oo;
+  }
+  __syncthreads();
+  const int l = ROW_IN ? tid / TPL : tid % L;
+  const int t = ROW_IN ? tid % TPL : tid / L;
+  const bool live = (g0 + l) < a.nlines;
+  const G* src = (const G*)a.src + offI[l];
+  const S* tw = (const S*)a.tw;
+
+  C v[8];
+#pragma unroll
+  for (int r = 0; r < 8; r++) {
+    v[r] = P::ld(src + (long long)(t + r * TPL) * a.sIa);
+    if (a.conj_in) v[r] = P::conj(v[r]);
+  }
+  bf8<P, SIGN>(v);  // stage 0 (Ns = 1, no twiddles)
+  S* cur = buf0;
+  S* nxt = buf1;
+  int Ns = 1;
+  // radix-8 stages 1 .. NS8-1 through shared memory (one barrier each)
+#pragma unroll
+  for (int s = 1; s < NS8; s++) {
+    {
+      const int k = t % Ns;
+      const int base = (t - k) * 8 + k;
+#pragma unroll
+      for (int r = 0; r < 8; r++) cur[l * LSP + pad(base + r * Ns)] = P::sts(P::renorm(v[r]));
+    }
+    __syncthreads();
+    Ns *= 8;
+#pragma unroll
+    for (int r = 0; r < 8; r++) v[r] = P::lds(cur[l * LSP + pad(t + r * TPL)]);
+    const int k = t % Ns;
+    const int step = N / (Ns * 8);
+#pragma unroll
+    for (int r = 1; r < 8; r++) v[r] = P::mul(v[r], P::twc(tw[k * r * step], SIGN));
+    bf8<P, SIGN>(v);
+    S* tmp = cur;
+    cur = nxt;
+    nxt = tmp;
+  }
+  G* dst = (G*)a.dst + offO[l];
+  if (Q == 1) {
+    // v holds the last stage (Ns = N/8, k = t): outputs y[t + r*TPL]
+    if (ROW_IN == ROW_OUT) {
+      if (live) {
+#pragma unroll
+        for (int r = 0; r < 8; r++) {
+          C o = a.conj_out ? P::conj(v[r]) : v[r];
+          P::st(dst + (long long)(t + r * TPL) * a.sOa, o);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int r = 0; r < 8; r++) cur[l * LSP + pad(t + r * TPL)] = P::sts(v[r]);
+    }
+  } else {
+    // radix-Q stage (Q = 2 or 4) with Ns = N/Q: butterflies j = t + b*TPL, k = j
+    {
+      const int k = t % Ns;
+      const int base = (t - k) * 8 + k;
+#pragma unroll
+      for (int r = 0; r < 8; r++) cur[l * LSP + pad(base + r * Ns)] = P::sts(P::renorm(v[r]));
+    }
+    __syncthreads();
+    constexpr int NB = 8 / Q;
+    constexpr int NQ = N / Q;
+    C w[8];
+#pragma unroll
+    for (int b = 0; b < NB; b++) {
+      const int j = t + b * TPL;
+#pragma unroll
+      for (int r = 0; r < Q; r++) {
+        C x = P::lds(cur[l * LSP + pad(j + r * NQ)]);
+        if (r > 0) x = P::mul(x, P::twc(tw[j * r], SIGN));
+        w[b * Q + r] = x;
+      }
+      if (Q == 2) {
+        C x0 = w[b * 2], x1 = w[b * 2 + 1];
+        w[b * 2] = P::add(x0, x1);
+        w[b * 2 + 1] = P::sub(x0, x1);
+      } else {
+        bf4<P, SIGN>(w[b * Q], w[b * Q + 1], w[b * Q + 2], w[b * Q + 3]);
+      }
+    }
+    if (ROW_IN == ROW_OUT) {
+      if (live) {
+#pragma unroll
+        for (int b = 0; b < NB; b++)
+#pragma unroll
+          for (int r = 0; r < Q; r++) {
+            C o = a.conj_out ? P::conj(w[b * Q + r]) : w[b * Q + r];
+            P::st(dst + (long long)(t + b * TPL + r * NQ) * a.sOa, o);
+          }
+      }
+    } else {
+#pragma unroll
+      for (int b = 0; b < NB; b++)
+#pragma unroll
+        for (int r = 0; r < Q; r++) nxt[l * LSP + pad(t + b * TPL + r * NQ)] = P::sts(w[b * Q + r]);
+      cur = nxt;
+    }
+  }
+  if (ROW_IN != ROW_OUT) {
+    __syncthreads();
+    // re-map threads to the output's contiguous direction
+    const int l2 = ROW_OUT ? tid / TPL : tid % L;
+    const int t2 = ROW_OUT ? tid % TPL : tid / L;
+    if ((g0 + l2) < a.nlines) {
+      G* d2 = (G*)a.dst + offO[l2];
+#pragma unroll
+      for (int r = 0; r < 8; r++) {
+        const int k = t2 + r * TPL;
+        C o = P::lds(cur[l2 * LSP + pad(k)]);
+        if (a.conj_out) o = P::conj(o);
+        P::st(d2 + (long long)k * a.sOa, o);
+      }
+    }
+  }
+}
+
+template <class P, int SIGN, int N, int L>
+int launch4(const FastArgs& a, bool row_in, bool row_out, cudaStream_t s) {
+  constexpr int T = L * (N / 8);
+  size_t smem = 16 * L + 2 * (size_t)L * (N + N / 8) * sizeof(typename P::S);
+  long long grid = (a.nlines + L - 1) / L;
+  if (grid > 2147483647LL) return (int)cudaErrorInvalidConfiguration;
+  cudaError_t e = cudaSuccess;
+#define PG_FAST_LAUNCH(RI, RO)                                                                       \
+  do {                                                                                             \
+    e = cudaFuncSetAttribute(k_fast<P, SIGN, N, L, RI, RO>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                             (int)smem);                                                           \
+    if (e != cudaSuccess) return (int)e;                                                           \
+    k_fast<P, SIGN, N, L, RI, RO><<<(unsigned)grid, T, smem, s>>>(a);                              \
+  } while (0)
+  if (row_in && row_out)
+    PG_FAST_LAUNCH(true, true);
+  else if (!row_in && !row_out)
+    PG_FAST_LAUNCH(false, false);
+  else if (row_in)
+    PG_FAST_LAUNCH(true, false);
+  else
+    PG_FAST_LAUNCH(false, true);
+#undef PG_FAST_LAUNCH
+  return (int)cudaGetLastError();
+}
+
+// Launchers, one explicit instantiation set per translation unit
+// (fft_fast_<arith>_<dir>_<range>.cu) so the build compiles them in parallel.
+template <class P, int SIGN>
+int launch_small(int N, const FastArgs& a, bool row_in, bool row_out, cudaStream_t s);
+template <class P, int SIGN>
+int launch_large(int N, const FastArgs& a, bool row_in, bool row_out, cudaStream_t s);
+
+}  // namespace fast
+}  // namespace pg

@@ -1,0 +1,22 @@
+// Instantiation unit of the register-resident pass kernel (see fft_fast.cuh).
+#include "fft_fast.cuh"
+
+namespace pg {
+namespace fast {
+
+template <class P, int SIGN>
+int launch_small(int N, const FastArgs& a, bool row_in, bool row_out, cudaStream_t s) {
+  const bool col = !(row_in && row_out);
+  switch (N) {
+    case 64: return launch4<P, SIGN, 64, 32>(a, row_in, row_out, s);
+    case 128: return launch4<P, SIGN, 128, 16>(a, row_in, row_out, s);
+    case 256: return launch4<P, SIGN, 256, 8>(a, row_in, row_out, s);
+    case 512: return col ? launch4<P, SIGN, 512, 8>(a, row_in, row_out, s) : launch4<P, SIGN, 512, 4>(a, row_in, row_out, s);
+  }
+  return -1;
+}
+
+template int launch_small<F32, -1>(int, const FastArgs&, bool, bool, cudaStream_t);
+
+}  // namespace fast
+}  // namespace pg
