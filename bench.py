@@ -198,6 +198,8 @@ def main():
     ap.add_argument("--ref-sample-n0", type=int, default=128)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--n", type=int, default=512, help="cube edge (profiling runs use a smaller case)")
+    ap.add_argument("--prec", default="double", choices=["double", "float"],
+                    help="double = pfft_ (complex128, the headline); float = pfftf_ (complex64)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup(args)
@@ -214,32 +216,36 @@ def main():
     cnt = int(np.prod(n))
     rng = np.random.default_rng(1 + rank)
     host = torch.from_numpy(rng.uniform(-1.0, 1.0, 2 * cnt))
+    pre = "pfft_" if args.prec == "double" else "pfftf_"
+    esz = 16 if args.prec == "double" else 8
+    if args.prec == "float":
+        host = host.float()
     a = host.to(dev)
     b = torch.empty_like(a)
     comm = pg.procmesh(2)
-    plan = L.pfft_plan_dft_3d(pg.ints(n), a.data_ptr(), b.data_ptr(), comm, pg.PFFT_FORWARD,
-                              pg.PFFT_TRANSPOSED_NONE | pg.PFFT_MEASURE)
+    plan = getattr(L, pre + "plan_dft_3d")(pg.ints(n), a.data_ptr(), b.data_ptr(), comm, pg.PFFT_FORWARD,
+                                           pg.PFFT_TRANSPOSED_NONE | pg.PFFT_MEASURE)
     if not plan:
         raise RuntimeError("plan failed: %s" % (pg.last_error(),))
     stream = torch.cuda.Stream(device=dev)
-    L.pfft_gb300_set_stream(plan, ctypes.c_void_p(stream.cuda_stream))
-    L.pfft_gb300_set_sync(plan, 0)
+    getattr(L, pre + "gb300_set_stream")(plan, ctypes.c_void_p(stream.cuda_stream))
+    getattr(L, pre + "gb300_set_sync")(plan, 0)
     npass = ctypes.c_int(0)
-    L.pfft_gb300_plan_info(plan, ctypes.byref(npass), None, None)
+    getattr(L, pre + "gb300_plan_info")(plan, ctypes.byref(npass), None, None)
     pass_bytes = []
     for i in range(npass.value):
         bb = ctypes.c_double(0)
-        L.pfft_gb300_pass_info(plan, i, None, None, None, None, None, ctypes.byref(bb))
+        getattr(L, pre + "gb300_pass_info")(plan, i, None, None, None, None, None, ctypes.byref(bb))
         pass_bytes.append(bb.value)
 
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
-            L.pfft_execute(plan)
+            getattr(L, pre + "execute")(plan)
     torch.cuda.synchronize()
 
     # ---- timed region: device-resident arrays ----
-    L.pfft_gb300_set_pass_timing(plan, 1)
-    L.pfft_gb300_set_sync(plan, 1)
+    getattr(L, pre + "gb300_set_pass_timing")(plan, 1)
+    getattr(L, pre + "gb300_set_sync")(plan, 1)
     clocks = Clocks(local)
     clocks.start()
     time.sleep(0.3)
@@ -249,7 +255,7 @@ def main():
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(args.steps):
-        L.pfft_execute(plan)
+        getattr(L, pre + "execute")(plan)
     e1.record(stream)
     torch.cuda.synchronize()
     barrier(world)
@@ -259,9 +265,9 @@ def main():
     for i in range(npass.value):
         t = ctypes.c_double(0)
         runs = ctypes.c_int(0)
-        L.pfft_gb300_pass_time(plan, i, ctypes.byref(t), ctypes.byref(runs))
+        getattr(L, pre + "gb300_pass_time")(plan, i, ctypes.byref(t), ctypes.byref(runs))
         pass_ms.append(t.value / max(1, runs.value))
-    L.pfft_gb300_set_pass_timing(plan, 0)
+    getattr(L, pre + "gb300_set_pass_timing")(plan, 0)
     ms_max = reduce_max(ms, world)
 
     # ---- e2e: pinned host arrays through the same C-ABI call ----
@@ -269,17 +275,19 @@ def main():
     if args.e2e_steps > 0:
         hin = host.pin_memory()
         hout = torch.empty_like(hin).pin_memory()
-        L.pfft_execute_dft(plan, hin.data_ptr(), hout.data_ptr())  # staging buffers allocated here, untimed
+        getattr(L, pre + "execute_dft")(plan, hin.data_ptr(), hout.data_ptr())  # staging buffers allocated here, untimed
         torch.cuda.synchronize()
         barrier(world)
         t0 = time.perf_counter()
         for _ in range(args.e2e_steps):
-            L.pfft_execute_dft(plan, hin.data_ptr(), hout.data_ptr())
+            getattr(L, pre + "execute_dft")(plan, hin.data_ptr(), hout.data_ptr())
         e2e_s = (time.perf_counter() - t0) / args.e2e_steps
         e2e_max = reduce_max(e2e_s, world)
-    L.pfft_destroy_plan(plan)
+    getattr(L, pre + "destroy_plan")(plan)
 
-    B = algo_bytes(n) if n == N3 else 2 * int(np.prod(n)) * ELEM * len(pass_ms)
+    pts = int(np.prod(n))
+    pmin = int(np.ceil(np.log2(pts) / (13 if esz == 16 else 14)))  # minimal HBM passes
+    B = pmin * 2 * pts * esz
     peak, peak_kind = measured_peak()
     value = world * B / (ms_max * 1e-3) / 1e9
     # dominant kernel: the pass with the largest share of the step
@@ -293,10 +301,12 @@ def main():
         "metric": "3D FFT HBM GB/s & %roofline, 5N*log2N GFLOP/s; batched vs loop; adjoint cost",
         "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64 storage, float-float arithmetic" if L.pfft_gb300_get_double_arith() == 0 else "f64",
+        "dtype": ("f32" if args.prec == "float" else
+                  "f64 storage, float-float arithmetic" if L.pfft_gb300_get_double_arith() == 0 else "f64"),
         "data": "synthetic uniform[-1,1) seed 1+rank",
-        "config": {"workload": "pfft_execute c2c 512^3 complex128 forward, 1x1 procmesh, out-of-place, "
-                               "TRANSPOSED_NONE", "bytes_per_step": B, "p_min": P_MIN,
+        "config": {"workload": "pfft_execute c2c %d^3 %s forward, 1x1 procmesh, out-of-place, "
+                               "TRANSPOSED_NONE" % (args.n, "complex128" if args.prec == "double" else "complex64"),
+                   "bytes_per_step": B, "p_min": pmin,
                    "l2": "arrays (2.1 GB) larger than L2; no flush", "parallelism": "replicas" if world > 1
                    else "single GPU"},
         "pct_roofline": value / world / peak,
@@ -306,8 +316,8 @@ def main():
                      "frac": (ach / peak) if ach else None, "traffic": traffic,
                      "kernel": "k_pass (pass %d of %d)" % (k, len(pass_ms)), "peak_source": peak_kind},
         "e2e": None if e2e_max is None else {
-            "value": world * B / e2e_max / 1e9, "unit": "GB/s", "h2d_bytes_per_step": 2 * cnt * 8,
-            "d2h_bytes_per_step": 2 * cnt * 8, "ms_per_step": e2e_max * 1e3},
+            "value": world * B / e2e_max / 1e9, "unit": "GB/s", "h2d_bytes_per_step": cnt * esz,
+            "d2h_bytes_per_step": cnt * esz, "ms_per_step": e2e_max * 1e3},
         "gpu_launches": npass.value * args.steps,
         "clocks": clk,
     }

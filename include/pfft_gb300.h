@@ -58,6 +58,27 @@ int pfftf_gb300_set_pass_timing(pfftf_plan plan, int on);
 int pfft_gb300_pass_time(const pfft_plan plan, int i, double *ms_total, int *runs);
 int pfftf_gb300_pass_time(const pfftf_plan plan, int i, double *ms_total, int *runs);
 
+/* Batched execution: many plans (uneven sizes, one precision) run as one
+ * persistent launch - a work queue of (plan, pass, tile) entries with
+ * per-plan pass dependencies - replayed from a CUDA graph.  Each plan runs on
+ * the arrays it was planned with.  batch_execute returns 0, a CUDA error, or
+ * -2 if a dependency wait timed out (the kernel bounds every wait). */
+typedef struct pfft_gb300_batch_s *pfft_gb300_batch;
+pfft_gb300_batch pfft_gb300_batch_create(int nplans, const pfft_plan *plans);
+pfft_gb300_batch pfftf_gb300_batch_create(int nplans, const pfftf_plan *plans);
+int pfft_gb300_batch_execute(pfft_gb300_batch batch);
+int pfft_gb300_batch_set_stream(pfft_gb300_batch batch, void *stream);
+int pfft_gb300_batch_set_graph(pfft_gb300_batch batch, int graph);
+int pfft_gb300_batch_info(pfft_gb300_batch batch, int *ntasks, int *grid, int *threads, double *bytes);
+void pfft_gb300_batch_destroy(pfft_gb300_batch batch);
+/* Test hook: runs the batch kernel on a queue whose dependency is never met,
+ * with the given wait limit; returns -2 when the bounded wait expired. */
+int pfft_gb300_batch_wait_selftest(long long spin_limit);
+
+/* Test hook: the double -> float-float -> double conversion of the double
+ * API's kernels, element by element (device arrays, queued on `stream`). */
+int pfft_gb300_selftest_df_roundtrip(const double *in, double *out, long long n, void *stream);
+
 /* Arithmetic of the double API: 0 = float-float on the FP32 pipes (default),
  * 1 = native FP64.  Applies to plans created afterwards. */
 void pfft_gb300_set_double_arith(int mode);

@@ -164,6 +164,18 @@ def _declare(L):
         f("gb300_pass_info").restype = ctypes.c_int
         f("gb300_pass_info").argtypes = [c_void_p, ctypes.c_int, _IP, _IP, _IP, _IP, _IP,
                                          ctypes.POINTER(ctypes.c_double)]
+    L.pfft_gb300_batch_create.restype = c_void_p
+    L.pfft_gb300_batch_create.argtypes = [ctypes.c_int, ctypes.POINTER(c_void_p)]
+    L.pfftf_gb300_batch_create.restype = c_void_p
+    L.pfftf_gb300_batch_create.argtypes = [ctypes.c_int, ctypes.POINTER(c_void_p)]
+    L.pfft_gb300_batch_execute.restype = ctypes.c_int
+    L.pfft_gb300_batch_execute.argtypes = [c_void_p]
+    L.pfft_gb300_batch_set_stream.argtypes = [c_void_p, c_void_p]
+    L.pfft_gb300_batch_set_graph.argtypes = [c_void_p, ctypes.c_int]
+    L.pfft_gb300_batch_info.argtypes = [c_void_p, _IP, _IP, _IP, ctypes.POINTER(ctypes.c_double)]
+    L.pfft_gb300_batch_destroy.argtypes = [c_void_p]
+    L.pfft_gb300_batch_wait_selftest.restype = ctypes.c_int
+    L.pfft_gb300_batch_wait_selftest.argtypes = [ctypes.c_longlong]
     L.pfft_gb300_last_error.restype = ctypes.c_int
     L.pfft_gb300_last_error_string.restype = ctypes.c_char_p
     L.pfft_gb300_set_double_arith.argtypes = [ctypes.c_int]

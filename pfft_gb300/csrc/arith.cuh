@@ -76,28 +76,29 @@ __device__ __forceinline__ df df_mul_add(df a, df b, df c, df d) {
 #define PG_DF_CONST(c) (::pg::df{(float)(c), (float)((c) - (double)(float)(c))})
 
 // double -> float-float using integer operations only.
-// hi is the double with its mantissa truncated to 24 bits; lo is the rounded
-// remainder.  Magnitudes outside [2^-126, 2^127] are flushed (to 0 / inf);
-// below 2^-74 the lo part underflows and the relative precision degrades to
-// single precision.
+// hi is the double with its mantissa truncated to 24 bits; lo is the
+// remainder, truncated to 24 bits (so hi + lo carries 48 of the 53 bits).
+// Magnitudes outside [2^-126, 2^127] are flushed (to 0 / inf); below 2^-74
+// the lo part underflows and the relative precision degrades to single
+// precision.
 __device__ __forceinline__ df df_from_double(double x) {
-  unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  unsigned sign = (unsigned)(b >> 63) << 31;
-  int e = (int)((b >> 52) & 0x7FF);
-  unsigned long long m = b & 0xFFFFFFFFFFFFFull;
-  int ef = e - 896;  // float biased exponent
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned h32 = (unsigned)(b >> 32), l32 = (unsigned)b;
+  const unsigned sign = h32 & 0x80000000u;
+  const int e = (int)((h32 >> 20) & 0x7FF);
+  const int ef = e - 896;  // float biased exponent
   if (ef <= 0) return {__uint_as_float(sign), 0.f};
   if (ef >= 255) return {__uint_as_float(sign | 0x7F800000u), 0.f};
-  float hi = __uint_as_float(sign | ((unsigned)ef << 23) | (unsigned)(m >> 29));
-  unsigned r = (unsigned)(m & 0x1FFFFFFFull);  // 29 low bits
-  // exact conversion of the two parts of r (6 + 23 bits) via the 2^23 trick
-  float rh = __fsub_rn(__uint_as_float(0x4B000000u | (r >> 23)), 8388608.f);
-  float rl = __fsub_rn(__uint_as_float(0x4B000000u | (r & 0x7FFFFFu)), 8388608.f);
-  float rf = __fmaf_rn(rh, 8388608.f, rl);  // one rounding
-  int es = e - 1075 + 127;                   // scale 2^(e-1075)
+  const float hi = __uint_as_float(sign | ((unsigned)ef << 23) | ((h32 & 0xFFFFFu) << 3) | (l32 >> 29));
+  const unsigned r = l32 & 0x1FFFFFFFu;  // the 29 bits below hi
   float lo = 0.f;
-  if (es > 0) lo = __fmul_rn(rf, __uint_as_float((unsigned)es << 23));
-  return {hi, sign ? -lo : lo};
+  if (r) {
+    const int lz = __clz(r);               // >= 3
+    const int fe = e - 917 - lz;           // biased exponent of r * 2^(e-1075)
+    const unsigned mn = (r << lz) >> 8;    // leading one at bit 23
+    if (fe > 0) lo = __uint_as_float(sign | ((unsigned)fe << 23) | (mn & 0x7FFFFFu));
+  }
+  return {hi, lo};
 }
 
 // float -> double bit pattern, exact, integer operations only (normal floats
@@ -111,45 +112,32 @@ __device__ __forceinline__ unsigned long long f2d_bits(float f) {
   return s | ((unsigned long long)(ef + 896) << 52) | ((unsigned long long)(u & 0x7FFFFF) << 29);
 }
 
-// float-float -> double (round toward zero on the last bits), integer ops only.
-// hi and lo are first merged into one 64-bit two's complement fixed-point
-// number in units of 2^(ehi-23-29), then normalised.
+// float-float -> double with integer operations only.  The pair is first
+// renormalised (|lo| <= ulp(hi)/2), so lo adds fewer than 2^29 units of the
+// double's last place to hi's 53-bit mantissa; low bits are truncated.
 __device__ __forceinline__ double df_to_double(df v) {
-  unsigned uh = __float_as_uint(v.hi);
-  unsigned eh = (uh >> 23) & 0xFF;
-  if (eh == 0) {
-    // hi is zero (or subnormal): fall back to lo alone
-    return __longlong_as_double((long long)f2d_bits(v.lo));
-  }
-  if (eh == 255) return __longlong_as_double((long long)f2d_bits(v.hi));
-  long long mh = (long long)((uh & 0x7FFFFF) | 0x800000) << 29;  // 53-bit magnitude
-  if (uh >> 31) mh = -mh;
-  unsigned ul = __float_as_uint(v.lo);
-  unsigned el = (ul >> 23) & 0xFF;
-  long long acc = mh;
+  const float hi = __fadd_rn(v.hi, v.lo);
+  const float lo = __fsub_rn(v.lo, __fsub_rn(hi, v.hi));
+  const unsigned uh = __float_as_uint(hi);
+  const unsigned eh = (uh >> 23) & 0xFF;
+  if (eh == 0 || eh == 255) return __longlong_as_double((long long)f2d_bits(hi));
+  const unsigned ul = __float_as_uint(lo);
+  const unsigned el = (ul >> 23) & 0xFF;
+  unsigned L = 0;
   if (el != 0) {
-    long long ml = (long long)((ul & 0x7FFFFF) | 0x800000);
-    int sh = (int)el - (int)eh + 29;  // lo mantissa weight relative to acc units
-    long long t;
-    if (sh >= 0) {
-      t = sh < 34 ? (ml << sh) : 0;  // |lo| cannot exceed |hi| much; guard anyway
-    } else {
-      t = sh > -25 ? (ml >> (-sh)) : 0;
-    }
-    acc += (ul >> 31) ? -t : t;
+    const unsigned ml = (ul & 0x7FFFFFu) | 0x800000u;
+    const int sh = (int)el - (int)eh + 29;  // <= 5
+    L = sh >= 0 ? (ml << sh) : (sh > -24 ? (ml >> (-sh)) : 0u);
   }
-  if (acc == 0) return 0.0;
-  unsigned long long s = 0;
-  unsigned long long a = (unsigned long long)acc;
-  if (acc < 0) {
-    s = 1ull << 63;
-    a = (unsigned long long)(-acc);
+  unsigned long long M = (unsigned long long)((uh & 0x7FFFFFu) | 0x800000u) << 29;
+  M = (((uh ^ ul) >> 31) == 0) ? M + L : M - L;
+  unsigned long long E = eh + 896;
+  if (M < (1ull << 52)) {  // a borrow moved the leading one down
+    M <<= 1;
+    E -= 1;
   }
-  int lz = __clzll((long long)a);  // a < 2^55
-  int shift = 11 - lz;             // bring leading 1 to bit 52
-  int e = (int)eh + 896 + shift;   // double biased exponent
-  unsigned long long mant = shift >= 0 ? (a >> shift) : (a << (-shift));
-  return __longlong_as_double((long long)(s | ((unsigned long long)e << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+  return __longlong_as_double((long long)(((unsigned long long)(uh >> 31) << 63) | (E << 52) |
+                                          (M & 0xFFFFFFFFFFFFFull)));
 }
 
 // ---------------------------------------------------------------------------
@@ -184,6 +172,8 @@ struct ArF32 {
   static __device__ __forceinline__ C lds(sm_t v) { return {v.x, v.y}; }
   static __device__ __forceinline__ sm_t sts(C v) { return make_float2(v.x, v.y); }
   static __device__ __forceinline__ C ldc(const gc_t* p) { gc_t v = *p; return {v.x, v.y}; }
+  static __device__ __forceinline__ C cvc(gc_t v) { return {v.x, v.y}; }
+  static __device__ __forceinline__ R cvr(gr_t v) { return v; }
   static __device__ __forceinline__ void stc(gc_t* p, C v) { *p = make_float2(v.x, v.y); }
   static __device__ __forceinline__ R ldr(const gr_t* p) { return *p; }
   static __device__ __forceinline__ void str(gr_t* p, R v) { *p = v; }
@@ -217,6 +207,8 @@ struct ArF64 {
   static __device__ __forceinline__ C lds(sm_t v) { return {v.x, v.y}; }
   static __device__ __forceinline__ sm_t sts(C v) { return make_double2(v.x, v.y); }
   static __device__ __forceinline__ C ldc(const gc_t* p) { gc_t v = *p; return {v.x, v.y}; }
+  static __device__ __forceinline__ C cvc(gc_t v) { return {v.x, v.y}; }
+  static __device__ __forceinline__ R cvr(gr_t v) { return v; }
   static __device__ __forceinline__ void stc(gc_t* p, C v) { *p = make_double2(v.x, v.y); }
   static __device__ __forceinline__ R ldr(const gr_t* p) { return *p; }
   static __device__ __forceinline__ void str(gr_t* p, R v) { *p = v; }
@@ -252,12 +244,24 @@ struct ArDF {
     gc_t v = *p;
     return {df_from_double(v.x), df_from_double(v.y)};
   }
+  static __device__ __forceinline__ C cvc(gc_t v) { return {df_from_double(v.x), df_from_double(v.y)}; }
+  static __device__ __forceinline__ R cvr(gr_t v) { return df_from_double(v); }
   static __device__ __forceinline__ void stc(gc_t* p, C v) {
     *p = make_double2(df_to_double(v.x), df_to_double(v.y));
   }
   static __device__ __forceinline__ R ldr(const gr_t* p) { return df_from_double(*p); }
   static __device__ __forceinline__ void str(gr_t* p, R v) { *p = df_to_double(v); }
 };
+
+// global load, optionally bypassing L1 (data written by other CTAs of the
+// same launch, published through a fence + counter)
+template <bool CG, class T>
+__device__ __forceinline__ T ldraw(const T* p) {
+  if constexpr (CG)
+    return __ldcg(p);
+  else
+    return *p;
+}
 
 // compile-time constant of the policy's real type
 template <class A>

@@ -1,0 +1,356 @@
+// Batched execution of many plans (of uneven sizes) in one persistent launch.
+//
+// Every pass of every plan is cut into tiles of L lines.  The tiles form one
+// work queue, ordered by pass level (all first passes, then all second
+// passes, ...).  A fixed grid of CTAs pulls tiles with an atomic ticket; a
+// tile of pass i of plan p first waits until all tiles of pass i-1 of the same
+// plan are done (a per-(plan, pass) counter), runs the generic pass tile, then
+// publishes its stores (fence) and bumps its own counter.  Tiles are dequeued
+// in order, so every tile a waiting CTA depends on is already held by a
+// running CTA: the queue cannot deadlock.  Each wait is bounded; on expiry the
+// kernel records an error word (read by the host) and carries on instead of
+// spinning forever.  Reads of data produced inside the launch go through L2
+// only (ld.global.cg), so no SM can see a stale L1 line.
+//
+// The launch (counter reset + kernel) is captured once into a CUDA graph and
+// replayed.
+#include <stdio.h>
+#include <string.h>
+#include <vector>
+#include "../../include/pfft.h"
+#include "../../include/pfft_gb300.h"
+#include "core.h"
+#include "pass_tile.cuh"
+
+using namespace pg;
+
+namespace {
+
+struct BatchTask {
+  int pass;   // index into the pass array
+  int tile;   // tile of that pass
+  int dep;    // counter to wait for (-1: none)
+  int need;   // value it must reach
+};
+
+struct BatchPass {
+  PassParams p;
+  int done;  // counter this pass increments
+};
+
+template <class A>
+__global__ void __launch_bounds__(512) k_batch(const BatchPass* __restrict__ passes,
+                                               const BatchTask* __restrict__ tasks, int ntasks,
+                                               unsigned* counters, unsigned* next, int* err,
+                                               long long spin_limit) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ int s_task;
+  for (;;) {
+    if (threadIdx.x == 0) s_task = (int)atomicAdd(next, 1u);
+    __syncthreads();
+    const int t = s_task;
+    __syncthreads();
+    if (t >= ntasks) break;
+    const BatchTask task = tasks[t];
+    const BatchPass& bp = passes[task.pass];
+    if (task.dep >= 0) {
+      if (threadIdx.x == 0) {
+        volatile unsigned* c = counters + task.dep;
+        long long it = 0;
+        while (*c < (unsigned)task.need) {
+          if (++it > spin_limit) {
+            atomicExch(err, 1);
+            break;
+          }
+          __nanosleep(100);
+        }
+        __threadfence();
+      }
+      __syncthreads();
+    }
+    if (bp.p.sign < 0)
+      pass_tile<A, -1, true>(bp.p, task.tile, smraw);
+    else
+      pass_tile<A, 1, true>(bp.p, task.tile, smraw);
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) atomicAdd(counters + bp.done, 1u);
+  }
+}
+
+struct Batch {
+  int arith = ARITH_DF;
+  std::vector<Plan*> plans;
+  BatchPass* d_passes = nullptr;
+  BatchTask* d_tasks = nullptr;
+  unsigned* d_counters = nullptr;  // ncounters + 1 (the last is the ticket)
+  int* d_err = nullptr;
+  int* h_err = nullptr;  // pinned
+  int ntasks = 0, ncounters = 0, threads = 64, smem = 0, grid = 1;
+  cudaStream_t stream = 0;
+  bool use_graph = true;
+  cudaGraphExec_t graph = nullptr;
+  double bytes = 0;
+};
+
+template <class A>
+const void* kernel_ptr() {
+  return (const void*)k_batch<A>;
+}
+
+const void* batch_kernel(int arith) {
+  switch (arith) {
+    case ARITH_F32: return kernel_ptr<ArF32>();
+    case ARITH_F64: return kernel_ptr<ArF64>();
+    default: return kernel_ptr<ArDF>();
+  }
+}
+
+int launch_batch(Batch* b, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(b->d_counters, 0, sizeof(unsigned) * (b->ncounters + 1), s);
+  if (e != cudaSuccess) return (int)e;
+  e = cudaMemsetAsync(b->d_err, 0, sizeof(int), s);
+  if (e != cudaSuccess) return (int)e;
+  const long long spin_limit = 20000000LL;  // ~2 s of 100 ns naps
+  unsigned* next = b->d_counters + b->ncounters;
+  switch (b->arith) {
+    case ARITH_F32:
+      k_batch<ArF32><<<b->grid, b->threads, b->smem, s>>>(b->d_passes, b->d_tasks, b->ntasks, b->d_counters, next,
+                                                          b->d_err, spin_limit);
+      break;
+    case ARITH_F64:
+      k_batch<ArF64><<<b->grid, b->threads, b->smem, s>>>(b->d_passes, b->d_tasks, b->ntasks, b->d_counters, next,
+                                                          b->d_err, spin_limit);
+      break;
+    default:
+      k_batch<ArDF><<<b->grid, b->threads, b->smem, s>>>(b->d_passes, b->d_tasks, b->ntasks, b->d_counters, next,
+                                                         b->d_err, spin_limit);
+  }
+  return (int)cudaGetLastError();
+}
+
+void free_batch(Batch* b) {
+  if (!b) return;
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  cudaFree(b->d_passes);
+  cudaFree(b->d_tasks);
+  cudaFree(b->d_counters);
+  cudaFree(b->d_err);
+  if (b->h_err) cudaFreeHost(b->h_err);
+  delete b;
+}
+
+Batch* make_batch(Plan* const* plans, int n) {
+  if (n < 1) return nullptr;
+  Batch* b = new Batch();
+  b->arith = plans[0]->arith;
+  std::vector<BatchPass> hp;
+  std::vector<int> first(n), npass(n);
+  int maxp = 0;
+  for (int i = 0; i < n; i++) {
+    Plan* pl = plans[i];
+    if (!pl || pl->arith != b->arith) {
+      report("batch: plans must be non-NULL and share their precision");
+      free_batch(b);
+      return nullptr;
+    }
+    b->plans.push_back(pl);
+    void* bufs[4] = {pl->in, pl->out, pl->ws[0], pl->ws[1]};
+    first[i] = (int)hp.size();
+    npass[i] = (int)pl->fwd.passes.size();
+    maxp = std::max(maxp, npass[i]);
+    for (const Pass& ps : pl->fwd.passes) {
+      BatchPass bp;
+      bp.p = ps.p;
+      bp.p.src = bufs[ps.src];
+      bp.p.dst = bufs[ps.dst];
+      cudaError_t e;
+      bp.p.tw = twiddle_table(ps.p.M, b->arith, &e);
+      if (!bp.p.tw) {
+        cuda_check(e, "batch twiddles");
+        free_batch(b);
+        return nullptr;
+      }
+      bp.done = (int)hp.size();
+      b->threads = std::max(b->threads, ps.p.threads);
+      b->smem = std::max(b->smem, ps.p.smem_bytes);
+      b->bytes += ps.bytes;
+      hp.push_back(bp);
+    }
+  }
+  b->ncounters = (int)hp.size();
+  std::vector<BatchTask> tasks;
+  for (int lvl = 0; lvl < maxp; lvl++)
+    for (int i = 0; i < n; i++) {
+      if (lvl >= npass[i]) continue;
+      int pi = first[i] + lvl;
+      const PassParams& p = hp[pi].p;
+      long long tiles = (p.nlines + p.L - 1) / p.L;
+      int dep = lvl > 0 ? pi - 1 : -1;
+      int need = 0;
+      if (dep >= 0) {
+        const PassParams& q = hp[dep].p;
+        need = (int)((q.nlines + q.L - 1) / q.L);
+      }
+      for (long long t = 0; t < tiles; t++) tasks.push_back({pi, (int)t, dep, need});
+    }
+  b->ntasks = (int)tasks.size();
+  const void* kfn = batch_kernel(b->arith);
+  if (cuda_check(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, b->smem), "batch attribute")) {
+    free_batch(b);
+    return nullptr;
+  }
+  int dev = 0, nsm = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kfn, b->threads, b->smem);
+  b->grid = std::max(1, std::min(b->ntasks, std::max(1, per) * nsm));
+  if (cuda_check(cudaMalloc(&b->d_passes, sizeof(BatchPass) * hp.size()), "batch alloc") ||
+      cuda_check(cudaMalloc(&b->d_tasks, sizeof(BatchTask) * tasks.size()), "batch alloc") ||
+      cuda_check(cudaMalloc(&b->d_counters, sizeof(unsigned) * (b->ncounters + 1)), "batch alloc") ||
+      cuda_check(cudaMalloc(&b->d_err, sizeof(int)), "batch alloc") ||
+      cuda_check(cudaMallocHost(&b->h_err, sizeof(int)), "batch alloc")) {
+    free_batch(b);
+    return nullptr;
+  }
+  cudaMemcpy(b->d_passes, hp.data(), sizeof(BatchPass) * hp.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(b->d_tasks, tasks.data(), sizeof(BatchTask) * tasks.size(), cudaMemcpyHostToDevice);
+  return b;
+}
+
+int run_batch(Batch* b) {
+  cudaStream_t s = b->stream;
+  int rc;
+  if (b->use_graph) {
+    if (!b->graph) {
+      cudaStream_t cs;
+      if (cuda_check(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "batch graph stream")) return -1;
+      cudaGraph_t g;
+      cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+      rc = launch_batch(b, cs);
+      cudaError_t ce = cudaStreamEndCapture(cs, &g);
+      cudaStreamDestroy(cs);
+      if (rc || ce != cudaSuccess) return cuda_check(rc ? (cudaError_t)rc : ce, "batch graph capture");
+      ce = cudaGraphInstantiate(&b->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (cuda_check(ce, "batch graph instantiate")) return -1;
+    }
+    rc = (int)cudaGraphLaunch(b->graph, s);
+  } else {
+    rc = launch_batch(b, s);
+  }
+  if (rc) return cuda_check((cudaError_t)rc, "batch launch");
+  rc = (int)cudaMemcpyAsync(b->h_err, b->d_err, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (rc) return cuda_check((cudaError_t)rc, "batch status");
+  rc = (int)cudaStreamSynchronize(s);
+  if (rc) return cuda_check((cudaError_t)rc, "batch execute");
+  if (*b->h_err) {
+    report("batch: a dependency wait timed out");
+    return -2;
+  }
+  return 0;
+}
+
+}  // namespace
+
+struct pfft_gb300_batch_s {
+  Batch* b;
+};
+
+struct pfft_plan_s {
+  Plan* p;
+};
+struct pfftf_plan_s {
+  Plan* p;
+};
+
+extern "C" {
+
+pfft_gb300_batch pfft_gb300_batch_create(int nplans, const pfft_plan* plans) {
+  std::vector<Plan*> v;
+  for (int i = 0; i < nplans; i++) v.push_back(plans[i] ? plans[i]->p : nullptr);
+  Batch* b = make_batch(v.data(), nplans);
+  if (!b) return nullptr;
+  return new pfft_gb300_batch_s{b};
+}
+
+pfft_gb300_batch pfftf_gb300_batch_create(int nplans, const pfftf_plan* plans) {
+  std::vector<Plan*> v;
+  for (int i = 0; i < nplans; i++) v.push_back(plans[i] ? plans[i]->p : nullptr);
+  Batch* b = make_batch(v.data(), nplans);
+  if (!b) return nullptr;
+  return new pfft_gb300_batch_s{b};
+}
+
+int pfft_gb300_batch_execute(pfft_gb300_batch batch) {
+  if (!batch) return -1;
+  return run_batch(batch->b);
+}
+
+int pfft_gb300_batch_set_stream(pfft_gb300_batch batch, void* stream) {
+  if (!batch) return -1;
+  batch->b->stream = (cudaStream_t)stream;
+  return 0;
+}
+
+int pfft_gb300_batch_set_graph(pfft_gb300_batch batch, int on) {
+  if (!batch) return -1;
+  batch->b->use_graph = on != 0;
+  return 0;
+}
+
+int pfft_gb300_batch_info(pfft_gb300_batch batch, int* ntasks, int* grid, int* threads, double* bytes) {
+  if (!batch) return -1;
+  if (ntasks) *ntasks = batch->b->ntasks;
+  if (grid) *grid = batch->b->grid;
+  if (threads) *threads = batch->b->threads;
+  if (bytes) *bytes = batch->b->bytes;
+  return 0;
+}
+
+void pfft_gb300_batch_destroy(pfft_gb300_batch batch) {
+  if (!batch) return;
+  free_batch(batch->b);
+  delete batch;
+}
+
+// Runs the batch kernel on a one-task queue whose dependency counter nothing
+// increments, with a wait limit of `spin_limit` naps: the wait must expire,
+// the kernel must return, and the status must be -2 (timed out).  Used by the
+// tests to exercise the bounded wait without hanging anything.
+int pfft_gb300_batch_wait_selftest(long long spin_limit) {
+  BatchPass* dp = nullptr;
+  BatchTask* dt = nullptr;
+  unsigned* dc = nullptr;
+  int* de = nullptr;
+  int herr = 0, rc = 0;
+  BatchPass hp;
+  memset(&hp, 0, sizeof(hp));
+  hp.p.nlines = 0;  // an empty tile: nothing is read or written
+  hp.p.L = 1;
+  hp.p.M = 1;
+  hp.p.N = 1;
+  hp.p.sign = -1;
+  hp.done = 0;
+  BatchTask ht = {0, 0, 1, 1};  // waits for counter 1 to reach 1: never happens
+  if (cudaMalloc(&dp, sizeof(hp)) != cudaSuccess || cudaMalloc(&dt, sizeof(ht)) != cudaSuccess ||
+      cudaMalloc(&dc, 3 * sizeof(unsigned)) != cudaSuccess || cudaMalloc(&de, sizeof(int)) != cudaSuccess) {
+    rc = -1;
+  } else {
+    cudaMemcpy(dp, &hp, sizeof(hp), cudaMemcpyHostToDevice);
+    cudaMemcpy(dt, &ht, sizeof(ht), cudaMemcpyHostToDevice);
+    cudaMemset(dc, 0, 3 * sizeof(unsigned));
+    cudaMemset(de, 0, sizeof(int));
+    k_batch<ArF32><<<1, 64, 1024>>>(dp, dt, 1, dc, dc + 2, de, spin_limit);
+    if (cudaDeviceSynchronize() != cudaSuccess) rc = -1;
+    cudaMemcpy(&herr, de, sizeof(int), cudaMemcpyDeviceToHost);
+    if (!rc) rc = herr ? -2 : 0;
+  }
+  cudaFree(dp);
+  cudaFree(dt);
+  cudaFree(dc);
+  cudaFree(de);
+  return rc;
+}
+
+}  // extern "C"

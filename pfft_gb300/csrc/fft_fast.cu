@@ -30,6 +30,8 @@ int launch_fast_pass(const PassParams& p, int arith, cudaStream_t stream) {
   a.nlines = p.nlines;
   a.conj_in = p.conj_in;
   a.conj_out = p.conj_out;
+  a.in_df = p.in_df;
+  a.out_df = p.out_df;
   const bool row_in = p.sIa == 1, row_out = p.sOa == 1;
   // column mapping needs adjacent lines on that side
   if (!row_in && !(p.nb > 0 && p.bsI[0] == 1)) return -1;

@@ -178,11 +178,43 @@ struct FastArgs {
   long long bsO[PG_MAX_BATCH];
   long long nlines;
   int conj_in, conj_out;
+  int in_df, out_df;  // double API: the array holds float-float pairs (an intermediate)
 };
 
+// global element access: native format, or float-float pairs for the
+// intermediate arrays of the double API (same 16 bytes per complex value)
+template <class P>
+__device__ __forceinline__ typename P::C gload(const typename P::G* p, int df);
+template <>
+__device__ __forceinline__ F32::C gload<F32>(const F32::G* p, int) { return *p; }
+template <>
+__device__ __forceinline__ FDD::C gload<FDD>(const FDD::G* p, int df) {
+  if (df) {
+    float4 v = *(const float4*)p;
+    return {{v.x, v.y}, {v.z, v.w}};
+  }
+  return FDD::ld(p);
+}
+template <class P>
+__device__ __forceinline__ void gstore(typename P::G* p, typename P::C v, int df);
+template <>
+__device__ __forceinline__ void gstore<F32>(F32::G* p, F32::C v, int) { *p = v; }
+template <>
+__device__ __forceinline__ void gstore<FDD>(FDD::G* p, FDD::C v, int df) {
+  if (df) {
+    FDD::C n = FDD::renorm(v);
+    *(float4*)p = make_float4(n.x.hi, n.x.lo, n.y.hi, n.y.lo);
+  } else {
+    FDD::st(p, v);
+  }
+}
+
 // ROW_IN: the axis is contiguous on the input side (thread t walks the line);
-// otherwise consecutive threads take consecutive lines.  ROW_OUT likewise for
-// the output; when they differ the last stage goes through shared memory.
+// otherwise consecutive threads take consecutive (adjacent) lines.  ROW_OUT
+// likewise for the output; when they differ the last stage is re-staged
+// through shared memory so that both sides stay coalesced.
+// Shared memory: one buffer of L lines, line stride N + N/8 + 1 (odd, so the
+// lines of a warp fall on different banks), index p + p/8 within a line.
 template <class P, int SIGN, int N, int L, bool ROW_IN, bool ROW_OUT>
 __global__ void __launch_bounds__(L*(N / 8)) k_fast(const FastArgs a) {
   typedef typename P::C C;
@@ -191,18 +223,17 @@ __global__ void __launch_bounds__(L*(N / 8)) k_fast(const FastArgs a) {
   constexpr int TPL = N / 8;  // threads per line
   constexpr int NS8 = n8_of(N);
   constexpr int Q = N / pow8(NS8);  // last radix: 1, 2 or 4
-  constexpr int LSP = N + N / 8;    // padded line stride in shared memory
+  constexpr int LSP = N + N / 8 + 1;
   extern __shared__ __align__(16) unsigned char sm_raw[];
   long long* offI = (long long*)sm_raw;
   long long* offO = offI + L;
-  S* buf0 = (S*)(sm_raw + 16 * L);
-  S* buf1 = buf0 + L * LSP;
+  S* buf = (S*)(sm_raw + 16 * L);
 
   const int tid = threadIdx.x;
   const long long g0 = (long long)blockIdx.x * L;
   if (tid < L) {
     long long g = g0 + tid;
-    if (g >= a.nlines) g = a.nlines - 1;  // tail CTA: clamp (duplicate work, same values)
+    if (g >= a.nlines) g = a.nlines - 1;  // tail CTA: clamp (duplicate work, never stored)
     long long oi = 0, oo = 0;
     for (int b = 0; b < a.nb; b++) {
       long long e = a.bext[b];
@@ -218,63 +249,63 @@ __global__ void __launch_bounds__(L*(N / 8)) k_fast(const FastArgs a) {
   const int l = ROW_IN ? tid / TPL : tid % L;
   const int t = ROW_IN ? tid % TPL : tid / L;
   const bool live = (g0 + l) < a.nlines;
-  const G* src = (const G*)a.src + offI[l];
   const S* tw = (const S*)a.tw;
+  S* line = buf + l * LSP;
 
   C v[8];
+  {
+    const G* src = (const G*)a.src + offI[l] + (long long)t * a.sIa;
+    const long long st = (long long)TPL * a.sIa;
 #pragma unroll
-  for (int r = 0; r < 8; r++) {
-    v[r] = P::ld(src + (long long)(t + r * TPL) * a.sIa);
-    if (a.conj_in) v[r] = P::conj(v[r]);
+    for (int r = 0; r < 8; r++) {
+      v[r] = gload<P>(src + r * st, a.in_df);
+      if (a.conj_in) v[r] = P::conj(v[r]);
+    }
   }
   bf8<P, SIGN>(v);  // stage 0 (Ns = 1, no twiddles)
-  S* cur = buf0;
-  S* nxt = buf1;
   int Ns = 1;
-  // radix-8 stages 1 .. NS8-1 through shared memory (one barrier each)
+  // radix-8 stages 1 .. NS8-1 through shared memory
 #pragma unroll
   for (int s = 1; s < NS8; s++) {
+    if (s > 1) __syncthreads();  // previous stage's loads are done
     {
       const int k = t % Ns;
       const int base = (t - k) * 8 + k;
 #pragma unroll
-      for (int r = 0; r < 8; r++) cur[l * LSP + pad(base + r * Ns)] = P::sts(P::renorm(v[r]));
+      for (int r = 0; r < 8; r++) line[pad(base + r * Ns)] = P::sts(P::renorm(v[r]));
     }
     __syncthreads();
     Ns *= 8;
 #pragma unroll
-    for (int r = 0; r < 8; r++) v[r] = P::lds(cur[l * LSP + pad(t + r * TPL)]);
+    for (int r = 0; r < 8; r++) v[r] = P::lds(line[pad(t + r * TPL)]);
     const int k = t % Ns;
     const int step = N / (Ns * 8);
 #pragma unroll
-    for (int r = 1; r < 8; r++) v[r] = P::mul(v[r], P::twc(tw[k * r * step], SIGN));
+    for (int r = 1; r < 8; r++) v[r] = P::mul(v[r], P::twc(__ldg(&tw[k * r * step]), SIGN));
     bf8<P, SIGN>(v);
-    S* tmp = cur;
-    cur = nxt;
-    nxt = tmp;
   }
-  G* dst = (G*)a.dst + offO[l];
   if (Q == 1) {
     // v holds the last stage (Ns = N/8, k = t): outputs y[t + r*TPL]
     if (ROW_IN == ROW_OUT) {
       if (live) {
+        G* dst = (G*)a.dst + offO[l] + (long long)t * a.sOa;
+        const long long st = (long long)TPL * a.sOa;
 #pragma unroll
-        for (int r = 0; r < 8; r++) {
-          C o = a.conj_out ? P::conj(v[r]) : v[r];
-          P::st(dst + (long long)(t + r * TPL) * a.sOa, o);
-        }
+        for (int r = 0; r < 8; r++) gstore<P>(dst + r * st, a.conj_out ? P::conj(v[r]) : v[r], a.out_df);
       }
-    } else {
-#pragma unroll
-      for (int r = 0; r < 8; r++) cur[l * LSP + pad(t + r * TPL)] = P::sts(v[r]);
+      return;
     }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < 8; r++) line[pad(t + r * TPL)] = P::sts(P::renorm(v[r]));
   } else {
     // radix-Q stage (Q = 2 or 4) with Ns = N/Q: butterflies j = t + b*TPL, k = j
+    if (NS8 > 1) __syncthreads();
     {
       const int k = t % Ns;
       const int base = (t - k) * 8 + k;
 #pragma unroll
-      for (int r = 0; r < 8; r++) cur[l * LSP + pad(base + r * Ns)] = P::sts(P::renorm(v[r]));
+      for (int r = 0; r < 8; r++) line[pad(base + r * Ns)] = P::sts(P::renorm(v[r]));
     }
     __syncthreads();
     constexpr int NB = 8 / Q;
@@ -285,8 +316,8 @@ __global__ void __launch_bounds__(L*(N / 8)) k_fast(const FastArgs a) {
       const int j = t + b * TPL;
 #pragma unroll
       for (int r = 0; r < Q; r++) {
-        C x = P::lds(cur[l * LSP + pad(j + r * NQ)]);
-        if (r > 0) x = P::mul(x, P::twc(tw[j * r], SIGN));
+        C x = P::lds(line[pad(j + r * NQ)]);
+        if (r > 0) x = P::mul(x, P::twc(__ldg(&tw[j * r]), SIGN));
         w[b * Q + r] = x;
       }
       if (Q == 2) {
@@ -299,35 +330,37 @@ __global__ void __launch_bounds__(L*(N / 8)) k_fast(const FastArgs a) {
     }
     if (ROW_IN == ROW_OUT) {
       if (live) {
+        G* dst = (G*)a.dst + offO[l];
 #pragma unroll
         for (int b = 0; b < NB; b++)
 #pragma unroll
           for (int r = 0; r < Q; r++) {
             C o = a.conj_out ? P::conj(w[b * Q + r]) : w[b * Q + r];
-            P::st(dst + (long long)(t + b * TPL + r * NQ) * a.sOa, o);
+            gstore<P>(dst + (long long)(t + b * TPL + r * NQ) * a.sOa, o, a.out_df);
           }
       }
-    } else {
-#pragma unroll
-      for (int b = 0; b < NB; b++)
-#pragma unroll
-        for (int r = 0; r < Q; r++) nxt[l * LSP + pad(t + b * TPL + r * NQ)] = P::sts(w[b * Q + r]);
-      cur = nxt;
+      return;
     }
-  }
-  if (ROW_IN != ROW_OUT) {
     __syncthreads();
-    // re-map threads to the output's contiguous direction
+#pragma unroll
+    for (int b = 0; b < NB; b++)
+#pragma unroll
+      for (int r = 0; r < Q; r++) line[pad(t + b * TPL + r * NQ)] = P::sts(P::renorm(w[b * Q + r]));
+  }
+  // re-staged store with the output's thread mapping
+  __syncthreads();
+  {
     const int l2 = ROW_OUT ? tid / TPL : tid % L;
     const int t2 = ROW_OUT ? tid % TPL : tid / L;
     if ((g0 + l2) < a.nlines) {
       G* d2 = (G*)a.dst + offO[l2];
+      const S* line2 = buf + l2 * LSP;
 #pragma unroll
       for (int r = 0; r < 8; r++) {
         const int k = t2 + r * TPL;
-        C o = P::lds(cur[l2 * LSP + pad(k)]);
+        C o = P::lds(line2[pad(k)]);
         if (a.conj_out) o = P::conj(o);
-        P::st(d2 + (long long)k * a.sOa, o);
+        gstore<P>(d2 + (long long)k * a.sOa, o, a.out_df);
       }
     }
   }
@@ -336,16 +369,21 @@ __global__ void __launch_bounds__(L*(N / 8)) k_fast(const FastArgs a) {
 template <class P, int SIGN, int N, int L>
 int launch4(const FastArgs& a, bool row_in, bool row_out, cudaStream_t s) {
   constexpr int T = L * (N / 8);
-  size_t smem = 16 * L + 2 * (size_t)L * (N + N / 8) * sizeof(typename P::S);
+  const size_t smem = 16 * L + (size_t)L * (N + N / 8 + 1) * sizeof(typename P::S);
   long long grid = (a.nlines + L - 1) / L;
   if (grid > 2147483647LL) return (int)cudaErrorInvalidConfiguration;
   cudaError_t e = cudaSuccess;
-#define PG_FAST_LAUNCH(RI, RO)                                                                       \
-  do {                                                                                             \
-    e = cudaFuncSetAttribute(k_fast<P, SIGN, N, L, RI, RO>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                             (int)smem);                                                           \
-    if (e != cudaSuccess) return (int)e;                                                           \
-    k_fast<P, SIGN, N, L, RI, RO><<<(unsigned)grid, T, smem, s>>>(a);                              \
+  // the attribute is set once per kernel instantiation
+#define PG_FAST_LAUNCH(RI, RO)                                                                            \
+  do {                                                                                                    \
+    static bool attr_done = false;                                                                        \
+    if (!attr_done) {                                                                                     \
+      e = cudaFuncSetAttribute(k_fast<P, SIGN, N, L, RI, RO>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                               (int)smem);                                                                \
+      if (e != cudaSuccess) return (int)e;                                                                \
+      attr_done = true;                                                                                   \
+    }                                                                                                     \
+    k_fast<P, SIGN, N, L, RI, RO><<<(unsigned)grid, T, smem, s>>>(a);                                     \
   } while (0)
   if (row_in && row_out)
     PG_FAST_LAUNCH(true, true);

@@ -72,6 +72,7 @@ struct PassParams {
   int wmode;    // adjoint weights: 1 = halve interior half-spectrum bins on load
                 // (C2R), 2 = double interior bins on store (R2C)
   int in_contig, out_contig;  // axis has unit stride on that side
+  int in_df, out_df;  // double API: complex array held as float-float pairs (intermediates)
   int threads;
   int smem_bytes;
 };

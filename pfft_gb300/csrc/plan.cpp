@@ -2,6 +2,7 @@
 #include <stdarg.h>
 #include <stdio.h>
 #include <string.h>
+#include <algorithm>
 #include <chrono>
 #include <mutex>
 #include <string>
@@ -211,7 +212,9 @@ void execute_plan(Plan* pl, void* in, void* out, bool adjoint) {
   if (!din || !dout) {
     // host arrays: stage through device buffers (copies are stream ordered)
     if (!din) {
-      if (!ensure_stage(pl, 0, bin)) return;
+      // an in-place host array also receives the output (and may hold
+      // intermediates up to the larger of the two layouts)
+      if (!ensure_stage(pl, 0, (pl->inplace && !dout) ? std::max(bin, bout) : bin)) return;
       xin = pl->stage[0];
       if (cuda_check(cudaMemcpyAsync(xin, in, bin, cudaMemcpyHostToDevice, s), "host-to-device copy")) return;
     }

@@ -471,24 +471,54 @@ bool build_program(const PlanDesc& d, int arith, bool inplace, bool adjoint, Pas
   }
 
   // ---- buffers: backwards from the output ---------------------------------------------
+  // Constraints: the last pass writes OUT; the input is never written; a pass
+  // whose source and destination are the same buffer must be in-place safe;
+  // an intermediate may live in OUT only if its layout fits in the output
+  // array (the caller's array may be exactly the output layout's size);
+  // everything else goes to the plan-owned workspaces (sized to fit).
   std::vector<int> dst(P);
   auto esz_in = [&](int i) { return mode_cplx_in(prog->passes[i].p.mode) ? esz_c : esz_r; };
   auto esz_out = [&](int i) { return mode_cplx_out(prog->passes[i].p.mode) ? esz_c : esz_r; };
+  auto lbytes = [&](const Layout& Lx) { return (size_t)Lx.span * (Lx.cplx ? esz_c : esz_r); };
+  const size_t cap_out = inplace ? std::max(lbytes(lay[0]), lbytes(lay[P])) : lbytes(lay[P]);
+  auto safe = [&](int i) { return inplace_safe(prog->passes[i].p, esz_in(i), esz_out(i)); };
   dst[P - 1] = BUF_OUT;
   for (int i = P - 2; i >= 0; i--) {
-    if (inplace_safe(prog->passes[i + 1].p, esz_in(i + 1), esz_out(i + 1)))
-      dst[i] = dst[i + 1];
-    else
-      dst[i] = (dst[i + 1] == BUF_OUT) ? BUF_WSA : (dst[i + 1] == BUF_WSA ? BUF_OUT : BUF_WSA);
+    const int cand[4] = {dst[i + 1], BUF_OUT, BUF_WSA, BUF_WSB};
+    dst[i] = -1;
+    for (int c : cand) {
+      if (c == dst[i + 1] && !safe(i + 1)) continue;
+      if (c == BUF_OUT && lbytes(lay[i + 1]) > cap_out) continue;
+      dst[i] = c;
+      break;
+    }
   }
-  if (inplace && dst[0] == BUF_OUT && !inplace_safe(prog->passes[0].p, esz_in(0), esz_out(0))) {
-    int nxt = (P > 1) ? dst[1] : BUF_OUT;
-    dst[0] = (nxt == BUF_WSA) ? BUF_WSB : BUF_WSA;
+  if (inplace && dst[0] == BUF_OUT && !safe(0)) {
+    if (P == 1) {
+      set_error(9, "this in-place transform needs an out-of-place array");
+      return false;
+    }
+    dst[0] = (dst[1] == BUF_WSA) ? BUF_WSB : BUF_WSA;
   }
-  // a pass must not read and write the same workspace unless it is safe
-  for (int i = 1; i < P; i++) {
-    if (dst[i] == dst[i - 1] && !inplace_safe(prog->passes[i].p, esz_in(i), esz_out(i))) {
-      dst[i - 1] = (dst[i] == BUF_WSA) ? BUF_WSB : BUF_WSA;
+  // self-check of the assignment
+  for (int i = 0; i < P; i++) {
+    int src = (i == 0) ? (inplace ? BUF_OUT : BUF_IN) : dst[i - 1];
+    bool ok = dst[i] >= BUF_OUT && (src != dst[i] || safe(i)) &&
+              (dst[i] != BUF_OUT || lbytes(lay[i + 1]) <= cap_out);
+    if (!ok) {
+      set_error(10, "internal error: invalid buffer assignment");
+      return false;
+    }
+  }
+  // double API: complex intermediates stay in float-float form between
+  // passes (same 16 bytes per value), so only the first pass converts from
+  // double and only the last converts back
+  if (arith == ARITH_DF) {
+    for (int i = 0; i + 1 < P; i++) {
+      if (lay[i + 1].cplx && mode_cplx_out(prog->passes[i].p.mode) && mode_cplx_in(prog->passes[i + 1].p.mode)) {
+        prog->passes[i].p.out_df = 1;
+        prog->passes[i + 1].p.in_df = 1;
+      }
     }
   }
   prog->ws_bytes[0] = prog->ws_bytes[1] = 0;
