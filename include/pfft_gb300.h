@@ -90,6 +90,26 @@ int pfft_gb300_get_double_arith(void);
 void pfft_gb300_set_kernel_path(int path);
 int pfft_gb300_get_kernel_path(void);
 
+/* Ghost-cell exchange that allocates nothing.  No counterpart in the
+ * reference PFFT.  For callers that cannot allocate device memory when they
+ * need the halo (solver loops that pre-size every buffer, memory-pool budgets,
+ * code that must not let cudaMalloc/cudaFree synchronise the device):
+ * the same periodic-wrap exchange as a ghost-cell plan's pfft_exchange, for a
+ * 3-D block of n[0] x n[1] x n[2] cells with `tuple` reals per cell (1 for
+ * real data, 2 for complex, times howmany) stored at the start of `data`,
+ * expanded in place into the (gc_below + n + gc_above) box.  precision: 1 =
+ * double, 0 = float.  `data` must be device or managed memory; `stream` is a
+ * cudaStream_t (NULL: the legacy default stream); the call only queues work.
+ * Scratch: a fixed 32 MiB array in the library's device image (every GPU that
+ * loads this code holds it until exit); blocks larger than 32 MiB are refused
+ * (cudaErrorMemoryAllocation returned, nothing queued).  The first call on a
+ * device looks up the array's device address; make that first call before
+ * any stream capture.  All calls share the array: calls whose GPU work
+ * overlaps (different streams, no ordering) race.  Returns 0 or a
+ * cudaError_t value. */
+int pfft_gb300_exchange_noalloc(int precision, const ptrdiff_t *n, const ptrdiff_t *gc_below,
+                                const ptrdiff_t *gc_above, ptrdiff_t tuple, void *data, void *stream);
+
 /* Last error (CUDA error code or library error) and its message. */
 int pfft_gb300_last_error(void);
 const char *pfft_gb300_last_error_string(void);
