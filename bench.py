@@ -68,7 +68,8 @@ def committed_traffic():
 
 
 class Clocks:
-    """Sample SM clocks and throttle reasons with nvidia-smi while running."""
+    """Sample SM clocks and throttle reasons with nvidia-smi every 50 ms; only
+    the samples stamped inside the timed window are kept."""
 
     def __init__(self, gpu=0):
         self.gpu = gpu
@@ -77,12 +78,12 @@ class Clocks:
         self.thread = None
 
     def start(self):
-        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+        q = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
              "clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
@@ -94,7 +95,8 @@ class Clocks:
         self.thread = threading.Thread(target=rd, daemon=True)
         self.thread.start()
 
-    def stop(self):
+    def stop(self, t0=None, t1=None):
+        """t0, t1: wall-clock (time.time()) bounds of the timed window."""
         if self.proc is None:
             return None
         self.proc.terminate()
@@ -104,21 +106,26 @@ class Clocks:
             self.proc.kill()
         if self.thread:
             self.thread.join(timeout=2)
-        sm, mx, reasons = [], None, set()
+        sm, mx, reasons, pw = [], None, set(), []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for s in self.samples:
             try:
-                sm.append(float(s[0]))
-                mx = float(s[1])
+                ts = time.mktime(time.strptime(s[0].split(".")[0], "%Y/%m/%d %H:%M:%S")) + \
+                    float("0." + s[0].split(".")[1]) if "." in s[0] else 0.0
+                if t0 is not None and not (t0 - 0.05 <= ts <= t1 + 0.05):
+                    continue
+                sm.append(float(s[1]))
+                mx = float(s[2])
+                pw.append(float(s[3]))
                 for i, nm in enumerate(names):
-                    if s[3 + i].lower().startswith("active"):
+                    if s[4 + i].lower().startswith("active"):
                         reasons.add(nm)
             except Exception:
                 continue
         if not sm:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "power_w_median": statistics.median(pw) if pw else None}
 
 
 def cpu_baseline(sample_n0=128, threads=None):
@@ -134,6 +141,127 @@ def cpu_baseline(sample_n0=128, threads=None):
     return {"value": algo_bytes(n) / dt / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
             "sample": "%dx512x512 c2c complex128 forward (1/%d of the workload), one run, %.2f s" %
                       (sample_n0, N3[0] // sample_n0, dt)}
+
+
+BATCH_SIZES = [(32, 32, 32), (48, 64, 40), (96, 96, 96), (128, 128, 64), (128, 128, 128)]
+
+
+def measure_batched(L, pg, torch, prec, nplans=64, seed=11, reps=5):
+    """64 uneven c2c transforms (sizes drawn by seed from BATCH_SIZES): one
+    persistent batched launch (CUDA graph) against a per-plan loop of plain
+    pfft_execute calls (blocking, as the reference's execute) and against the
+    same loop queued asynchronously on one stream; returns times, ratios and
+    the largest relative difference between the batch and the loop outputs."""
+    pre = "pfft_" if prec == "double" else "pfftf_"
+    cdt = torch.complex128 if prec == "double" else torch.complex64
+    rng = np.random.default_rng(seed)
+    comm = pg.procmesh(2)
+    plans, outs, pts = [], [], 0
+    for _ in range(nplans):
+        n = BATCH_SIZES[int(rng.integers(0, len(BATCH_SIZES)))]
+        x = torch.from_numpy(rng.uniform(-1, 1, 2 * int(np.prod(n)))).view(torch.complex128).to(cdt).cuda()
+        y = torch.zeros_like(x)
+        p = getattr(L, pre + "plan_dft_3d")(pg.ints(n), x.data_ptr(), y.data_ptr(), comm, pg.PFFT_FORWARD, 0)
+        if not p:
+            raise RuntimeError("plan failed: %s" % (pg.last_error(),))
+        plans.append((p, x, y))
+        outs.append(y)
+        pts += int(np.prod(n))
+    ex = getattr(L, pre + "execute")
+    s0 = torch.cuda.default_stream()
+
+    def timed(fn):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s0)
+        for _ in range(reps):
+            fn()
+        e1.record(s0)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    def loop():
+        for p, _, _ in plans:
+            ex(p)
+    loop_ms = timed(loop)
+    ref = [y.clone() for y in outs]
+    for p, _, _ in plans:
+        getattr(L, pre + "gb300_set_sync")(p, 0)
+    loop_async_ms = timed(loop)
+    for p, _, _ in plans:
+        getattr(L, pre + "gb300_set_sync")(p, 1)
+    arr = (ctypes.c_void_p * nplans)(*[p for p, _, _ in plans])
+    b = getattr(L, pre + "gb300_batch_create")(nplans, arr)
+    if not b:
+        raise RuntimeError("batch failed: %s" % (pg.last_error(),))
+    for y in outs:
+        y.zero_()
+
+    def batch():
+        if L.pfft_gb300_batch_execute(b) != 0:
+            raise RuntimeError("batch execute failed: %s" % (pg.last_error(),))
+    batch_ms = timed(batch)
+    ntasks, grid = ctypes.c_int(0), ctypes.c_int(0)
+    L.pfft_gb300_batch_info(b, ctypes.byref(ntasks), ctypes.byref(grid), None, None)
+    diff = max(float(torch.linalg.vector_norm(y - r) / torch.linalg.vector_norm(r)) for y, r in zip(outs, ref))
+    L.pfft_gb300_batch_destroy(b)
+    for p, _, _ in plans:
+        getattr(L, pre + "destroy_plan")(p)
+    esz = 16 if prec == "double" else 8
+    return {"transforms": nplans, "points": pts, "dtype": "complex128" if prec == "double" else "complex64",
+            "batch_ms": batch_ms, "loop_ms": loop_ms, "loop_async_ms": loop_async_ms,
+            "ratio": loop_ms / batch_ms, "ratio_vs_async_loop": loop_async_ms / batch_ms,
+            "batch_gbs_min_traffic": 3 * 2 * pts * esz / (batch_ms * 1e-3) / 1e9,
+            "max_rel_l2_batch_vs_loop": diff, "tasks": ntasks.value, "grid": grid.value}
+
+
+def measure_adjoint(L, pg, torch, reps=5):
+    """Cost of a forward+adjoint gradient step through the C-ABI against two
+    plain executes, on the differentiable oversampled r2c (float32 128^3
+    zero-padded to 256^3) and on the 512^3 c2c complex128 transform."""
+    res = {}
+    comm = pg.procmesh(2)
+    s = torch.cuda.Stream()
+    cases = [("r2c_f32_128to256", "pfftf_", 3, (256, 256, 256), (128, 128, 128)),
+             ("c2c_f64_512", "pfft_", 3, (512, 512, 512), (512, 512, 512))]
+    for name, pre, d, n, ni in cases:
+        a = [pg.ints([0] * d) for _ in range(4)]
+        kind = "r2c" if name.startswith("r2c") else "c2c"
+        ls = "local_size_many_dft_r2c" if kind == "r2c" else "local_size_many_dft"
+        alloc = getattr(L, pre + ls)(d, pg.ints(n), pg.ints(ni), pg.ints(n), 1, None, None, comm, 0, *a)
+        x = torch.zeros(2 * alloc, dtype=torch.float64 if pre == "pfft_" else torch.float32, device="cuda")
+        y = torch.zeros_like(x)
+        x.uniform_(-1, 1)
+        pl = "plan_many_dft_r2c" if kind == "r2c" else "plan_many_dft"
+        p = getattr(L, pre + pl)(d, pg.ints(n), pg.ints(ni), pg.ints(n), 1, None, None, x.data_ptr(), y.data_ptr(),
+                                 comm, pg.PFFT_FORWARD, 0)
+        if not p:
+            raise RuntimeError("plan failed: %s" % (pg.last_error(),))
+        getattr(L, pre + "gb300_set_stream")(p, ctypes.c_void_p(s.cuda_stream))
+        getattr(L, pre + "gb300_set_sync")(p, 0)
+        ex, adj = getattr(L, pre + "execute"), getattr(L, pre + "execute_adjoint")
+
+        def timed(fn):
+            for _ in range(3):
+                fn()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            for _ in range(reps):
+                fn()
+            e1.record(s)
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1) / reps
+
+        two = timed(lambda: (ex(p), ex(p)))
+        fa = timed(lambda: (ex(p), adj(p)))
+        getattr(L, pre + "destroy_plan")(p)
+        res[name] = {"fwd_adj_ms": fa, "two_exec_ms": two, "ratio": fa / two}
+        del x, y
+        torch.cuda.empty_cache()
+    return res
 
 
 def dist_setup(args):
@@ -191,10 +319,11 @@ def run_reference(args, world, rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the batched-vs-loop and adjoint-cost parts")
     ap.add_argument("--ref-sample-n0", type=int, default=128)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--n", type=int, default=512, help="cube edge (profiling runs use a smaller case)")
@@ -232,7 +361,9 @@ def main():
     getattr(L, pre + "gb300_set_sync")(plan, 0)
     npass = ctypes.c_int(0)
     getattr(L, pre + "gb300_plan_info")(plan, ctypes.byref(npass), None, None)
+    plan_arith = getattr(L, pre + "gb300_plan_arith")(plan)
     pass_bytes = []
+    pass_kernel = [getattr(L, pre + "gb300_pass_kernel")(plan, i) for i in range(npass.value)]
     for i in range(npass.value):
         bb = ctypes.c_double(0)
         getattr(L, pre + "gb300_pass_info")(plan, i, None, None, None, None, None, ctypes.byref(bb))
@@ -248,19 +379,21 @@ def main():
     getattr(L, pre + "gb300_set_sync")(plan, 1)
     clocks = Clocks(local)
     clocks.start()
-    time.sleep(0.3)
+    time.sleep(0.5)
     barrier(world)
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
+    tw0 = time.time()
     e0.record(stream)
     for _ in range(args.steps):
         getattr(L, pre + "execute")(plan)
     e1.record(stream)
     torch.cuda.synchronize()
+    tw1 = time.time()
     barrier(world)
     ms = e0.elapsed_time(e1) / args.steps
-    clk = clocks.stop()
+    clk = clocks.stop(tw0, tw1)
     pass_ms = []
     for i in range(npass.value):
         t = ctypes.c_double(0)
@@ -284,6 +417,14 @@ def main():
         e2e_s = (time.perf_counter() - t0) / args.e2e_steps
         e2e_max = reduce_max(e2e_s, world)
     getattr(L, pre + "destroy_plan")(plan)
+    del a, b
+    torch.cuda.empty_cache()
+
+    # ---- the metric's other two parts: batched vs loop, adjoint cost (untimed by the step clock) ----
+    extra = {}
+    if not args.no_extras:
+        extra["batched_vs_loop"] = {pr: measure_batched(L, pg, torch, pr) for pr in ("double", "float")}
+        extra["adjoint_cost"] = measure_adjoint(L, pg, torch)
 
     pts = int(np.prod(n))
     pmin = int(np.ceil(np.log2(pts) / (13 if esz == 16 else 14)))  # minimal HBM passes
@@ -301,8 +442,7 @@ def main():
         "metric": "3D FFT HBM GB/s & %roofline, 5N*log2N GFLOP/s; batched vs loop; adjoint cost",
         "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": ("f32" if args.prec == "float" else
-                  "f64 storage, float-float arithmetic" if L.pfft_gb300_get_double_arith() == 0 else "f64"),
+        "dtype": {0: "f32", 1: "f64", 2: "f64 storage, float-float arithmetic"}[plan_arith],
         "data": "synthetic uniform[-1,1) seed 1+rank",
         "config": {"workload": "pfft_execute c2c %d^3 %s forward, 1x1 procmesh, out-of-place, "
                                "TRANSPOSED_NONE" % (args.n, "complex128" if args.prec == "double" else "complex64"),
@@ -314,13 +454,15 @@ def main():
         "pass_ms": pass_ms,
         "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                      "frac": (ach / peak) if ach else None, "traffic": traffic,
-                     "kernel": "k_pass (pass %d of %d)" % (k, len(pass_ms)), "peak_source": peak_kind},
+                     "kernel": "%s (pass %d of %d)" % ("k_fast" if pass_kernel[k] == 1 else "k_pass", k, len(pass_ms)),
+                     "peak_source": peak_kind},
         "e2e": None if e2e_max is None else {
             "value": world * B / e2e_max / 1e9, "unit": "GB/s", "h2d_bytes_per_step": cnt * esz,
             "d2h_bytes_per_step": cnt * esz, "ms_per_step": e2e_max * 1e3},
         "gpu_launches": npass.value * args.steps,
         "clocks": clk,
     }
+    line.update(extra)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(sample_n0=args.ref_sample_n0)
     print(json.dumps(line), flush=True)

@@ -44,6 +44,13 @@ int pfftf_gb300_set_graph(pfftf_plan plan, int graph);
  * passes of elements read + written), and plan-owned workspace bytes. */
 int pfft_gb300_plan_info(const pfft_plan plan, int *npasses, double *bytes, size_t *ws_bytes);
 int pfftf_gb300_plan_info(const pfftf_plan plan, int *npasses, double *bytes, size_t *ws_bytes);
+/* Kernel of pass i: 1 = register-resident radix-8 kernel, 0 = general pass
+ * kernel, -1 = no such pass. */
+int pfft_gb300_pass_kernel(const pfft_plan plan, int i);
+int pfftf_gb300_pass_kernel(const pfftf_plan plan, int i);
+/* Arithmetic a plan runs in: 0 FP32 (float API), 1 native FP64, 2 float-float. */
+int pfft_gb300_plan_arith(const pfft_plan plan);
+int pfftf_gb300_plan_arith(const pfftf_plan plan);
 int pfft_gb300_pass_info(const pfft_plan plan, int i, int *axis, int *M, int *L, int *threads, int *smem,
                          double *bytes);
 int pfftf_gb300_pass_info(const pfftf_plan plan, int i, int *axis, int *M, int *L, int *threads, int *smem,
@@ -79,10 +86,33 @@ int pfft_gb300_batch_wait_selftest(long long spin_limit);
  * API's kernels, element by element (device arrays, queued on `stream`). */
 int pfft_gb300_selftest_df_roundtrip(const double *in, double *out, long long n, void *stream);
 
-/* Arithmetic of the double API: 0 = float-float on the FP32 pipes (default),
- * 1 = native FP64.  Applies to plans created afterwards. */
-void pfft_gb300_set_double_arith(int mode);
+/* Arithmetic of the double API, for plans created afterwards:
+ *   0  float-float on the FP32 pipes (48-49 significant bits; relative L2
+ *      error of a transform about 1e-15)
+ *   1  native FP64 (full double rounding; FP64 issues at about 1/64 of the
+ *      FP32 rate on GB300)
+ *   2  by size (default): native FP64 for transforms of at most 2^18 points
+ *      (howmany included), float-float above.
+ * The environment variable PFFT_GB300_F64_ARITH=df|native|auto sets the
+ * initial mode.  Returns 0, or -1 for an unknown mode. */
+int pfft_gb300_set_double_arith(int mode);
 int pfft_gb300_get_double_arith(void);
+
+/* Autotuning and wisdom.  Plans created with PFFT_PATIENT, PFFT_EXHAUSTIVE
+ * or PFFT_TUNE time the candidate configurations of every pass (radix-8
+ * kernel tile height; general kernel radix order and lines per CTA) on the
+ * planned arrays - overwriting the output array (and an in-place array), as
+ * FFTW's measuring planners do - and keep the fastest.  The choices are kept
+ * as wisdom, keyed by a complete description of the pass, and reused by any
+ * later plan with the same pass.  No counterpart in the reference's API (PFFT
+ * leaves wisdom to FFTW).  Import/export return 1 on success, 0 on failure;
+ * the exported string is released with free(). */
+char *pfft_gb300_export_wisdom_to_string(void);
+int pfft_gb300_import_wisdom_from_string(const char *wisdom);
+int pfft_gb300_export_wisdom_to_filename(const char *filename);
+int pfft_gb300_import_wisdom_from_filename(const char *filename);
+void pfft_gb300_forget_wisdom(void);
+int pfft_gb300_wisdom_entries(void);
 
 /* Kernel selection: 1 (default) runs power-of-two c2c passes on the
  * register-resident radix-8 kernel, 0 uses the general pass kernel everywhere

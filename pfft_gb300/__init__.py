@@ -179,9 +179,36 @@ def _declare(L):
     L.pfft_gb300_last_error.restype = ctypes.c_int
     L.pfft_gb300_last_error_string.restype = ctypes.c_char_p
     L.pfft_gb300_set_double_arith.argtypes = [ctypes.c_int]
+    L.pfft_gb300_set_double_arith.restype = ctypes.c_int
+    for nm in ("pfft_gb300_plan_arith", "pfftf_gb300_plan_arith"):
+        getattr(L, nm).argtypes = [c_void_p]
+        getattr(L, nm).restype = ctypes.c_int
+    L.pfft_gb300_export_wisdom_to_string.restype = c_void_p
+    L.pfft_gb300_import_wisdom_from_string.argtypes = [ctypes.c_char_p]
+    L.pfft_gb300_import_wisdom_from_string.restype = ctypes.c_int
+    L.pfft_gb300_export_wisdom_to_filename.argtypes = [ctypes.c_char_p]
+    L.pfft_gb300_export_wisdom_to_filename.restype = ctypes.c_int
+    L.pfft_gb300_import_wisdom_from_filename.argtypes = [ctypes.c_char_p]
+    L.pfft_gb300_import_wisdom_from_filename.restype = ctypes.c_int
+    L.pfft_gb300_wisdom_entries.restype = ctypes.c_int
+    for nm in ("pfft_gb300_pass_kernel", "pfftf_gb300_pass_kernel"):
+        getattr(L, nm).argtypes = [c_void_p, ctypes.c_int]
+        getattr(L, nm).restype = ctypes.c_int
     L.pfft_gb300_set_kernel_path.argtypes = [ctypes.c_int]
     L.pfft_gb300_get_kernel_path.restype = ctypes.c_int
     L.pfft_gb300_get_double_arith.restype = ctypes.c_int
+
+
+def export_wisdom():
+    """The wisdom of this process as text (see pfft_gb300_export_wisdom_to_string)."""
+    L = lib()
+    p = L.pfft_gb300_export_wisdom_to_string()
+    if not p:
+        return None
+    try:
+        return ctypes.string_at(p).decode()
+    finally:
+        ctypes.CDLL(None).free(ctypes.c_void_p(p))
 
 
 def lib():

@@ -1,8 +1,10 @@
 """Build libpfft_gb300.so (the C-ABI library) in-tree with nvcc for sm_103a.
 
 Every translation unit under pfft_gb300/csrc is compiled in parallel and
-linked into pfft_gb300/libpfft_gb300.so.  A unit is recompiled only when it
-or one of the headers is newer than its object file.
+linked into pfft_gb300/libpfft_gb300.so.  The batched-launch units
+(batch*.cu) are relocatable device code, device-linked together, so that the
+tile functions of the persistent kernel compile in parallel units.  A unit is
+recompiled only when it or one of the headers is newer than its object file.
 """
 import concurrent.futures as cf
 import glob
@@ -37,8 +39,16 @@ def _headers():
     return hs
 
 
+def _rdc(src):
+    return os.path.basename(src).startswith("batch")
+
+
 def _compile(src, extra):
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+    if _rdc(src):
+        extra = list(extra) + ["-rdc=true"]
+    if os.path.basename(src).startswith("batch_tiles"):
+        extra = list(extra) + ["-maxrregcount=128"]  # callees of a kernel bounded to two 256-thread blocks per SM
     newest_dep = max([os.path.getmtime(src)] + [os.path.getmtime(h) for h in _headers()])
     if os.path.exists(obj) and os.path.getmtime(obj) >= newest_dep:
         return obj, None
@@ -66,8 +76,14 @@ def build(verbose=False, extra=None):
     newest = max(os.path.getmtime(o) for o in objs)
     if not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
         libdir = _cuda_lib_dir()
-        cmd = [_nvcc()] + ARCH + ["-shared", "-cudart", "shared", "-o", LIB + ".tmp"] + objs + [
-            "-Xlinker", "-rpath," + libdir, "-L" + libdir]
+        rdc = [o for s_, o in zip(srcs, objs) if _rdc(s_)]
+        dlink = os.path.join(BUILD, "device_link.o")
+        cmd = [_nvcc()] + ARCH + ["-dlink", "-Xcompiler", "-fPIC", "-o", dlink] + rdc
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("device link failed: %s\n%s\n%s" % (" ".join(cmd), r.stdout, r.stderr))
+        cmd = [_nvcc()] + ARCH + ["-shared", "-cudart", "shared", "-o", LIB + ".tmp"] + objs + [dlink,
+            "-Xlinker", "--no-undefined", "-Xlinker", "-rpath," + libdir, "-L" + libdir]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed: %s\n%s\n%s" % (" ".join(cmd), r.stdout, r.stderr))

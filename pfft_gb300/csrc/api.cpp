@@ -367,6 +367,14 @@ void do_execute(Plan* pl, void* in, void* out) {
     if (ws_bytes) *ws_bytes = plan->p->ws_cap[0] + plan->p->ws_cap[1];                                    \
     return 0;                                                                                             \
   }                                                                                                       \
+  int PX##gb300_pass_kernel(const PX##plan plan, int i) {                                                \
+    if (!plan || i < 0 || i >= (int)plan->p->fwd.passes.size()) return -1;                                \
+    return fast_pass_eligible(plan->p->fwd.passes[i].p, plan->p->arith) ? 1 : 0;                         \
+  }                                                                                                       \
+  int PX##gb300_plan_arith(const PX##plan plan) {                                                        \
+    if (!plan) return -1;                                                                                 \
+    return plan->p->arith;                                                                                \
+  }                                                                                                       \
   int PX##gb300_pass_info(const PX##plan plan, int i, int* axis, int* M, int* L, int* threads,            \
                           int* smem, double* bytes) {                                                    \
     if (!plan || i < 0 || i >= (int)plan->p->fwd.passes.size()) return -1;                                \
@@ -403,6 +411,10 @@ const char* pfft_gb300_last_error_string(void) { return last_error_string(); }
 void pfft_gb300_clear_error(void) { clear_error(); }
 void pfft_gb300_set_kernel_path(int path) { set_kernel_path(path ? 1 : 0); }
 int pfft_gb300_get_kernel_path(void) { return kernel_path(); }
-void pfft_gb300_set_double_arith(int mode) { set_double_arith(mode == 1 ? ARITH_F64 : ARITH_DF); }
-int pfft_gb300_get_double_arith(void) { return double_arith() == ARITH_F64 ? 1 : 0; }
+int pfft_gb300_set_double_arith(int mode) {
+  if (mode != DARITH_DF && mode != DARITH_NATIVE && mode != DARITH_AUTO) return -1;
+  set_double_arith(mode);
+  return 0;
+}
+int pfft_gb300_get_double_arith(void) { return double_arith(); }
 }

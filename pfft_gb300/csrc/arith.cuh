@@ -75,28 +75,31 @@ __device__ __forceinline__ df df_mul_add(df a, df b, df c, df d) {
 // Used only on compile-time constants so no FP64 instruction is emitted.
 #define PG_DF_CONST(c) (::pg::df{(float)(c), (float)((c) - (double)(float)(c))})
 
-// double -> float-float using integer operations only.
-// hi is the double with its mantissa truncated to 24 bits; lo is the
-// remainder, truncated to 24 bits (so hi + lo carries 48 of the 53 bits).
-// Magnitudes outside [2^-126, 2^127] are flushed (to 0 / inf); below 2^-74
-// the lo part underflows and the relative precision degrades to single
-// precision.
+// double -> float-float with integer and exact float operations only (no
+// FP64 instruction, no leading-zero count, no branch).
+// hi is the double with its mantissa truncated to 24 bits: the exponent is
+// rebiased by bit arithmetic ((e - 896) mod 256 = low8(e) ^ 0x80).  The 29
+// remaining mantissa bits r are turned into floats exactly by subtracting two
+// floats of the same exponent, one with part of r in its mantissa field and
+// one without (lo1: bits 28..6 of r, lo2: bits 5..0); lo = lo1 + lo2 keeps 24
+// significant bits.  Magnitudes outside [2^-126, 2^127] are flushed (to 0 /
+// inf, NaN stays NaN when its payload has high bits); below 2^-80 lo2 and
+// below 2^-103 lo1 underflow, and the relative precision degrades to 2^-47
+// and 2^-24.
 __device__ __forceinline__ df df_from_double(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const unsigned h32 = (unsigned)(b >> 32), l32 = (unsigned)b;
+  const unsigned h32 = (unsigned)__double2hiint(x), l32 = (unsigned)__double2loint(x);
   const unsigned sign = h32 & 0x80000000u;
-  const int e = (int)((h32 >> 20) & 0x7FF);
-  const int ef = e - 896;  // float biased exponent
-  if (ef <= 0) return {__uint_as_float(sign), 0.f};
-  if (ef >= 255) return {__uint_as_float(sign | 0x7F800000u), 0.f};
-  const float hi = __uint_as_float(sign | ((unsigned)ef << 23) | ((h32 & 0xFFFFFu) << 3) | (l32 >> 29));
-  const unsigned r = l32 & 0x1FFFFFFFu;  // the 29 bits below hi
-  float lo = 0.f;
-  if (r) {
-    const int lz = __clz(r);               // >= 3
-    const int fe = e - 917 - lz;           // biased exponent of r * 2^(e-1075)
-    const unsigned mn = (r << lz) >> 8;    // leading one at bit 23
-    if (fe > 0) lo = __uint_as_float(sign | ((unsigned)fe << 23) | (mn & 0x7FFFFFu));
+  const unsigned e = (h32 >> 20) & 0x7FFu;
+  const unsigned t = (h32 << 3) | (l32 >> 29);  // low 9 bits of e, then the top 23 mantissa bits
+  float hi = __uint_as_float(((t & 0x7FFFFFFFu) ^ 0x40000000u) | sign);
+  const unsigned b1 = (((h32 & 0x7FF00000u) << 3) - (919u << 23)) | sign;  // 2^(e-1046), valid for e >= 920
+  const unsigned b2 = b1 - (23u << 23);                                      // 2^(e-1069), valid for e >= 943
+  const float lo1 = __fsub_rn(__uint_as_float(b1 | ((l32 >> 6) & 0x7FFFFFu)), __uint_as_float(b1));
+  const float lo2 = __fsub_rn(__uint_as_float(b2 | ((l32 & 63u) << 17)), __uint_as_float(b2));
+  float lo = e >= 943u ? __fadd_rn(lo1, lo2) : (e >= 920u ? lo1 : 0.f);
+  if (e - 897u >= 254u) {  // outside the float range: signed zero, inf or NaN
+    hi = __uint_as_float(e < 897u ? sign : (sign | 0x7F800000u | (t & 0x7FFFFFu)));
+    lo = 0.f;
   }
   return {hi, lo};
 }

@@ -1,132 +1,54 @@
-// Batched execution of many plans (of uneven sizes) in one persistent launch.
-//
-// Every pass of every plan is cut into tiles of L lines.  The tiles form one
-// work queue, ordered by pass level (all first passes, then all second
-// passes, ...).  A fixed grid of CTAs pulls tiles with an atomic ticket; a
-// tile of pass i of plan p first waits until all tiles of pass i-1 of the same
-// plan are done (a per-(plan, pass) counter), runs the generic pass tile, then
-// publishes its stores (fence) and bumps its own counter.  Tiles are dequeued
-// in order, so every tile a waiting CTA depends on is already held by a
-// running CTA: the queue cannot deadlock.  Each wait is bounded; on expiry the
-// kernel records an error word (read by the host) and carries on instead of
-// spinning forever.  Reads of data produced inside the launch go through L2
-// only (ld.global.cg), so no SM can see a stale L1 line.
+// Batched execution of many plans (of uneven sizes) in one persistent launch:
+// host side (work queue, dependency counters, CUDA graph).  The kernel is in
+// batch_kernel.cuh.
 //
 // The launch (counter reset + kernel) is captured once into a CUDA graph and
 // replayed.
 #include <stdio.h>
 #include <string.h>
+#include <algorithm>
 #include <vector>
 #include "../../include/pfft.h"
 #include "../../include/pfft_gb300.h"
+#include "batch_kernel.cuh"
 #include "core.h"
-#include "pass_tile.cuh"
 
 using namespace pg;
 
 namespace {
 
-struct BatchTask {
-  int pass;   // index into the pass array
-  int tile;   // tile of that pass
-  int dep;    // counter to wait for (-1: none)
-  int need;   // value it must reach
-};
-
-struct BatchPass {
-  PassParams p;
-  int done;  // counter this pass increments
-};
-
-template <class A>
-__global__ void __launch_bounds__(512) k_batch(const BatchPass* __restrict__ passes,
-                                               const BatchTask* __restrict__ tasks, int ntasks,
-                                               unsigned* counters, unsigned* next, int* err,
-                                               long long spin_limit) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  __shared__ int s_task;
-  for (;;) {
-    if (threadIdx.x == 0) s_task = (int)atomicAdd(next, 1u);
-    __syncthreads();
-    const int t = s_task;
-    __syncthreads();
-    if (t >= ntasks) break;
-    const BatchTask task = tasks[t];
-    const BatchPass& bp = passes[task.pass];
-    if (task.dep >= 0) {
-      if (threadIdx.x == 0) {
-        volatile unsigned* c = counters + task.dep;
-        long long it = 0;
-        while (*c < (unsigned)task.need) {
-          if (++it > spin_limit) {
-            atomicExch(err, 1);
-            break;
-          }
-          __nanosleep(100);
-        }
-        __threadfence();
-      }
-      __syncthreads();
-    }
-    if (bp.p.sign < 0)
-      pass_tile<A, -1, true>(bp.p, task.tile, smraw);
-    else
-      pass_tile<A, 1, true>(bp.p, task.tile, smraw);
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) atomicAdd(counters + bp.done, 1u);
-  }
-}
-
 struct Batch {
-  int arith = ARITH_DF;
+  int arith = ARITH_DF;  // ARITH_F32 for a float batch; a double batch mixes F64 and DF plans
   std::vector<Plan*> plans;
   BatchPass* d_passes = nullptr;
   BatchTask* d_tasks = nullptr;
   unsigned* d_counters = nullptr;  // ncounters + 1 (the last is the ticket)
   int* d_err = nullptr;
   int* h_err = nullptr;  // pinned
-  int ntasks = 0, ncounters = 0, threads = 64, smem = 0, grid = 1;
+  int ntasks = 0, ncounters = 0, threads = BATCH_THREADS, smem = 0, grid = 1;
+  int fast_passes = 0;
   cudaStream_t stream = 0;
   bool use_graph = true;
   cudaGraphExec_t graph = nullptr;
   double bytes = 0;
 };
 
-template <class A>
-const void* kernel_ptr() {
-  return (const void*)k_batch<A>;
-}
-
-const void* batch_kernel(int arith) {
-  switch (arith) {
-    case ARITH_F32: return kernel_ptr<ArF32>();
-    case ARITH_F64: return kernel_ptr<ArF64>();
-    default: return kernel_ptr<ArDF>();
-  }
-}
+const void* batch_kernel(int arith) { return arith == ARITH_F32 ? batch_kernel_f32() : batch_kernel_f64(); }
 
 int launch_batch(Batch* b, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(b->d_counters, 0, sizeof(unsigned) * (b->ncounters + 1), s);
   if (e != cudaSuccess) return (int)e;
   e = cudaMemsetAsync(b->d_err, 0, sizeof(int), s);
   if (e != cudaSuccess) return (int)e;
-  const long long spin_limit = 20000000LL;  // ~2 s of 100 ns naps
-  unsigned* next = b->d_counters + b->ncounters;
-  switch (b->arith) {
-    case ARITH_F32:
-      k_batch<ArF32><<<b->grid, b->threads, b->smem, s>>>(b->d_passes, b->d_tasks, b->ntasks, b->d_counters, next,
-                                                          b->d_err, spin_limit);
-      break;
-    case ARITH_F64:
-      k_batch<ArF64><<<b->grid, b->threads, b->smem, s>>>(b->d_passes, b->d_tasks, b->ntasks, b->d_counters, next,
-                                                          b->d_err, spin_limit);
-      break;
-    default:
-      k_batch<ArDF><<<b->grid, b->threads, b->smem, s>>>(b->d_passes, b->d_tasks, b->ntasks, b->d_counters, next,
-                                                         b->d_err, spin_limit);
-  }
-  return (int)cudaGetLastError();
+  BatchLaunch q;
+  q.passes = b->d_passes;
+  q.tasks = b->d_tasks;
+  q.ntasks = b->ntasks;
+  q.counters = b->d_counters;
+  q.next = b->d_counters + b->ncounters;
+  q.err = b->d_err;
+  q.spin_limit = 20000000LL;  // ~2 s of 100 ns naps
+  return b->arith == ARITH_F32 ? batch_launch_f32(q, b->grid, b->smem, s) : batch_launch_f64(q, b->grid, b->smem, s);
 }
 
 void free_batch(Batch* b) {
@@ -143,13 +65,15 @@ void free_batch(Batch* b) {
 Batch* make_batch(Plan* const* plans, int n) {
   if (n < 1) return nullptr;
   Batch* b = new Batch();
-  b->arith = plans[0]->arith;
+  b->arith = plans[0] && plans[0]->arith == ARITH_F32 ? ARITH_F32 : ARITH_DF;
   std::vector<BatchPass> hp;
+  std::vector<long long> ntiles;
   std::vector<int> first(n), npass(n);
   int maxp = 0;
+  const size_t fsz = b->arith == ARITH_F32 ? sizeof(float2) : sizeof(float4);
   for (int i = 0; i < n; i++) {
     Plan* pl = plans[i];
-    if (!pl || pl->arith != b->arith) {
+    if (!pl || (pl->arith == ARITH_F32) != (b->arith == ARITH_F32)) {
       report("batch: plans must be non-NULL and share their precision");
       free_batch(b);
       return nullptr;
@@ -161,21 +85,43 @@ Batch* make_batch(Plan* const* plans, int n) {
     maxp = std::max(maxp, npass[i]);
     for (const Pass& ps : pl->fwd.passes) {
       BatchPass bp;
+      memset(&bp, 0, sizeof(bp));
       bp.p = ps.p;
       bp.p.src = bufs[ps.src];
       bp.p.dst = bufs[ps.dst];
       cudaError_t e;
-      bp.p.tw = twiddle_table(ps.p.M, b->arith, &e);
+      bp.arith = pl->arith;
+      bp.p.tw = twiddle_table(ps.p.M, pl->arith, &e);
       if (!bp.p.tw) {
         cuda_check(e, "batch twiddles");
         free_batch(b);
         return nullptr;
       }
       bp.done = (int)hp.size();
-      b->threads = std::max(b->threads, ps.p.threads);
-      b->smem = std::max(b->smem, ps.p.smem_bytes);
+      // radix-8 tile when the pass qualifies (power-of-two c2c lines up to
+      // 512 with the same orientation on both sides), else a general tile
+      bool ri = false, ro = false;
+      long long tiles;
+      if (kernel_path() == 1 && ps.p.N <= 512 && fast::fast_args(bp.p, pl->arith, &bp.fa, &ri, &ro) && ri == ro) {
+        bp.fastN = ps.p.N;
+        bp.frow = ri ? 1 : 0;
+        const int L = batch_fast_lines(bp.fastN);
+        tiles = (ps.p.nlines + L - 1) / L;
+        b->smem = std::max(b->smem, (int)(16 * L + (size_t)L * (bp.fastN + bp.fastN / 8 + 1) * fsz));
+        b->fast_passes++;
+      } else {
+        bp.fastN = 0;
+        if (!fit_pass_threads(&bp.p, pl->arith, BATCH_THREADS)) {
+          report("batch: a pass needs more threads than the batched launch has");
+          free_batch(b);
+          return nullptr;
+        }
+        tiles = (bp.p.nlines + bp.p.L - 1) / bp.p.L;
+        b->smem = std::max(b->smem, bp.p.smem_bytes);
+      }
       b->bytes += ps.bytes;
       hp.push_back(bp);
+      ntiles.push_back(tiles);
     }
   }
   b->ncounters = (int)hp.size();
@@ -184,15 +130,9 @@ Batch* make_batch(Plan* const* plans, int n) {
     for (int i = 0; i < n; i++) {
       if (lvl >= npass[i]) continue;
       int pi = first[i] + lvl;
-      const PassParams& p = hp[pi].p;
-      long long tiles = (p.nlines + p.L - 1) / p.L;
       int dep = lvl > 0 ? pi - 1 : -1;
-      int need = 0;
-      if (dep >= 0) {
-        const PassParams& q = hp[dep].p;
-        need = (int)((q.nlines + q.L - 1) / q.L);
-      }
-      for (long long t = 0; t < tiles; t++) tasks.push_back({pi, (int)t, dep, need});
+      int need = dep >= 0 ? (int)ntiles[dep] : 0;
+      for (long long t = 0; t < ntiles[pi]; t++) tasks.push_back({pi, (int)t, dep, need});
     }
   b->ntasks = (int)tasks.size();
   const void* kfn = batch_kernel(b->arith);
@@ -203,7 +143,7 @@ Batch* make_batch(Plan* const* plans, int n) {
   int dev = 0, nsm = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kfn, b->threads, b->smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kfn, BATCH_THREADS, b->smem);
   b->grid = std::max(1, std::min(b->ntasks, std::max(1, per) * nsm));
   if (cuda_check(cudaMalloc(&b->d_passes, sizeof(BatchPass) * hp.size()), "batch alloc") ||
       cuda_check(cudaMalloc(&b->d_tasks, sizeof(BatchTask) * tasks.size()), "batch alloc") ||
@@ -341,8 +281,15 @@ int pfft_gb300_batch_wait_selftest(long long spin_limit) {
     cudaMemcpy(dt, &ht, sizeof(ht), cudaMemcpyHostToDevice);
     cudaMemset(dc, 0, 3 * sizeof(unsigned));
     cudaMemset(de, 0, sizeof(int));
-    k_batch<ArF32><<<1, 64, 1024>>>(dp, dt, 1, dc, dc + 2, de, spin_limit);
-    if (cudaDeviceSynchronize() != cudaSuccess) rc = -1;
+    BatchLaunch q;
+    q.passes = dp;
+    q.tasks = dt;
+    q.ntasks = 1;
+    q.counters = dc;
+    q.next = dc + 2;
+    q.err = de;
+    q.spin_limit = spin_limit;
+    if (batch_launch_f32(q, 1, 1024, 0) != 0 || cudaDeviceSynchronize() != cudaSuccess) rc = -1;
     cudaMemcpy(&herr, de, sizeof(int), cudaMemcpyDeviceToHost);
     if (!rc) rc = herr ? -2 : 0;
   }

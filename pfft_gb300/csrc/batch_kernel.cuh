@@ -1,0 +1,161 @@
+// Persistent kernel of the batched execution (host side: batch.cu).
+//
+// Every pass of every plan is cut into tiles; the tiles form one work queue,
+// ordered by pass level (all first passes, then all second passes, ...).  A
+// fixed grid of CTAs pulls tiles with an atomic ticket; a tile of pass i of
+// plan p first waits until all tiles of pass i-1 of the same plan are done (a
+// per-(plan, pass) counter), runs the tile, then publishes its stores (fence)
+// and bumps its own counter.  Tiles are dequeued in order, so every tile a
+// waiting CTA depends on is already held by a running CTA: the queue cannot
+// deadlock.  Each wait is bounded; on expiry the kernel records an error word
+// (read by the host) and carries on instead of spinning forever.  Reads of
+// data produced inside the launch go through L2 only (ld.global.cg), so no SM
+// can see a stale L1 line.
+//
+// A tile is either a register-resident radix-8 tile (power-of-two c2c lines
+// of 64..512 points, BATCH_THREADS = L * N/8 threads) or a general pass tile.
+// The batch_*.cu units are compiled as relocatable device code.
+#pragma once
+#include <type_traits>
+#include "fft_fast.cuh"
+#include "pass_tile.cuh"
+
+namespace pg {
+
+constexpr int BATCH_THREADS = 256;
+
+struct BatchTask {
+  int pass;   // index into the pass array
+  int tile;   // tile of that pass
+  int dep;    // counter to wait for (-1: none)
+  int need;   // value it must reach
+};
+
+struct BatchPass {
+  PassParams p;      // general tile parameters
+  fast::FastArgs fa; // radix-8 tile parameters (fastN > 0)
+  int fastN;         // line length of a radix-8 tile pass, 0 for a general tile
+  int frow;          // radix-8 tile: 1 = lines contiguous on both sides, 0 = columns
+  int done;          // counter this pass increments
+  int arith;         // arithmetic of the pass's plan
+};
+
+struct BatchLaunch {
+  const BatchPass* passes;
+  const BatchTask* tasks;
+  int ntasks;
+  unsigned* counters;
+  unsigned* next;
+  int* err;
+  long long spin_limit;
+};
+
+// lines per radix-8 tile at BATCH_THREADS threads
+__host__ __device__ constexpr int batch_fast_lines(int N) { return BATCH_THREADS * 8 / N; }
+
+// Radix-8 tiles are expanded inline (they are register-resident and short);
+// the general tiles are separate device functions in their own translation
+// units (batch_tiles_gen_*.cu, relocatable device code, at most 128 registers
+// so that two 256-thread blocks fit an SM): each is compiled once, in
+// parallel with the rest of the build.
+#define PG_BT_GEN(name) __device__ void name(const PassParams& p, long long tile, unsigned char* sm)
+PG_BT_GEN(bt_gen_f32_m);
+PG_BT_GEN(bt_gen_f32_p);
+PG_BT_GEN(bt_gen_df_m);
+PG_BT_GEN(bt_gen_df_p);
+PG_BT_GEN(bt_gen_f64_m);
+PG_BT_GEN(bt_gen_f64_p);
+#define PG_BT_DEF_GEN(name, A, SIGN) \
+  PG_BT_GEN(name) { pass_tile<A, SIGN, true>(p, tile, sm); }
+
+template <class P, int N>
+__device__ __forceinline__ void batch_fast_n(const BatchPass& bp, long long tile, unsigned char* sm) {
+  constexpr int L = batch_fast_lines(N);
+  if (bp.frow) {
+    if (bp.p.sign < 0)
+      fast::fast_tile<P, -1, N, L, true, true, true>(bp.fa, tile, sm);
+    else
+      fast::fast_tile<P, 1, N, L, true, true, true>(bp.fa, tile, sm);
+  } else {
+    if (bp.p.sign < 0)
+      fast::fast_tile<P, -1, N, L, false, false, true>(bp.fa, tile, sm);
+    else
+      fast::fast_tile<P, 1, N, L, false, false, true>(bp.fa, tile, sm);
+  }
+}
+
+template <bool DOUBLE>
+__device__ __forceinline__ void batch_fast(const BatchPass& bp, long long tile, unsigned char* sm) {
+  typedef typename std::conditional<DOUBLE, fast::FDD, fast::F32>::type P;
+  switch (bp.fastN) {
+    case 64: batch_fast_n<P, 64>(bp, tile, sm); break;
+    case 128: batch_fast_n<P, 128>(bp, tile, sm); break;
+    case 256: batch_fast_n<P, 256>(bp, tile, sm); break;
+    default: batch_fast_n<P, 512>(bp, tile, sm); break;
+  }
+}
+
+// Float batches (DOUBLE = false) run FP32 tiles; in a double batch every
+// pass carries its own arithmetic (native FP64 for small plans, float-float
+// for large ones).
+template <bool DOUBLE>
+__global__ void __launch_bounds__(BATCH_THREADS, 2) k_batch(const BatchLaunch q) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ int s_task;
+  for (;;) {
+    if (threadIdx.x == 0) s_task = (int)atomicAdd(q.next, 1u);
+    __syncthreads();
+    const int t = s_task;
+    __syncthreads();
+    if (t >= q.ntasks) break;
+    const BatchTask task = q.tasks[t];
+    const BatchPass& bp = q.passes[task.pass];
+    if (task.dep >= 0) {
+      if (threadIdx.x == 0) {
+        volatile unsigned* c = q.counters + task.dep;
+        long long it = 0;
+        while (*c < (unsigned)task.need) {
+          if (++it > q.spin_limit) {
+            atomicExch(q.err, 1);
+            break;
+          }
+          __nanosleep(100);
+        }
+        __threadfence();
+      }
+      __syncthreads();
+    }
+    const long long tile = task.tile;
+    unsigned char* sm = smraw;
+    const bool neg = bp.p.sign < 0;
+    if (bp.fastN > 0) {
+      batch_fast<DOUBLE>(bp, tile, sm);
+    } else if (!DOUBLE) {
+      if (neg)
+        bt_gen_f32_m(bp.p, tile, sm);
+      else
+        bt_gen_f32_p(bp.p, tile, sm);
+    } else if (bp.arith == ARITH_F64) {
+      if (neg)
+        bt_gen_f64_m(bp.p, tile, sm);
+      else
+        bt_gen_f64_p(bp.p, tile, sm);
+    } else {
+      if (neg)
+        bt_gen_df_m(bp.p, tile, sm);
+      else
+        bt_gen_df_p(bp.p, tile, sm);
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) atomicAdd(q.counters + bp.done, 1u);
+  }
+}
+
+// instantiation units batch_f32.cu / batch_f64.cu
+int batch_launch_f32(const BatchLaunch& q, int grid, int smem, cudaStream_t s);
+int batch_launch_f64(const BatchLaunch& q, int grid, int smem, cudaStream_t s);
+const void* batch_kernel_f32();
+const void* batch_kernel_f64();
+
+}  // namespace pg

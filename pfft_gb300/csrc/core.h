@@ -169,6 +169,14 @@ struct Plan {
 // Build the pass program of a plan (planner.cpp).  Returns false on failure
 // (message recorded with set_error).
 bool build_program(const PlanDesc& d, int arith, bool inplace, bool adjoint, PassProgram* prog);
+// Wisdom and autotuning (tune.cpp): apply recorded choices to a program;
+// time the candidates of every pass on the plan's arrays and record the best.
+void apply_wisdom(PassProgram* prog, int arith);
+bool tune_program(Plan* pl, PassProgram* prog);
+// Re-plan the general kernel of a pass (radix order, lines per CTA).
+bool refit_pass(PassParams* p, int arith, int pref, int L);
+// Re-fit a general pass to at most max_threads threads (batched launches).
+bool fit_pass_threads(PassParams* p, int arith, int max_threads);
 // Run a program with resolved buffers.  Returns a cudaError_t value.
 int run_program(Plan* pl, const PassProgram& prog, void* in, void* out, cudaStream_t s);
 // Ensure workspace capacity for a program.
@@ -179,8 +187,11 @@ Plan* make_plan(const PlanDesc& base, void* in, void* out);
 void execute_plan(Plan* pl, void* in, void* out, bool adjoint);
 void destroy_plan(Plan* pl);
 
-// arithmetic used for the double API (ARITH_DF by default)
+// arithmetic policy of the double API: float-float, native FP64, or by size
+enum { DARITH_DF = 0, DARITH_NATIVE = 1, DARITH_AUTO = 2 };
+constexpr long long DARITH_AUTO_POINTS = 1LL << 18;
 int double_arith();
 void set_double_arith(int a);
+int plan_double_arith(const PlanDesc& d);
 
 }  // namespace pg

@@ -3,40 +3,57 @@
 
 namespace pg {
 
+namespace fast {
+bool fast_args(const PassParams& p, int arith, FastArgs* a, bool* row_in, bool* row_out) {
+  if (p.mode != MODE_C2C || p.nst == 0) return false;
+  if (p.M != p.N || p.Ni != p.N || p.No != p.N || p.Zi || p.Zo || p.wmode) return false;
+  const int N = p.N;
+  if (N < 64 || N > 4096 || (N & (N - 1))) return false;
+  if (arith != ARITH_F32 && arith != ARITH_DF) return false;
+  if (p.ashI.en || p.ashO.en) return false;
+  if (p.nb > PG_MAX_BATCH) return false;
+  for (int b = 0; b < p.nb; b++)
+    if (p.bshI[b].en || p.bshO[b].en) return false;
+  a->src = p.src;
+  a->dst = p.dst;
+  a->tw = p.tw;
+  a->sIa = p.sIa;
+  a->sOa = p.sOa;
+  a->nb = p.nb;
+  for (int b = 0; b < p.nb; b++) {
+    a->bext[b] = p.bext[b];
+    a->bsI[b] = p.bsI[b];
+    a->bsO[b] = p.bsO[b];
+  }
+  a->nlines = p.nlines;
+  a->conj_in = p.conj_in;
+  a->conj_out = p.conj_out;
+  a->in_df = p.in_df;
+  a->out_df = p.out_df;
+  *row_in = p.sIa == 1;
+  *row_out = p.sOa == 1;
+  // column mapping needs adjacent lines on that side
+  if (!*row_in && !(p.nb > 0 && p.bsI[0] == 1)) return false;
+  if (!*row_out && !(p.nb > 0 && p.bsO[0] == 1)) return false;
+  return true;
+}
+}  // namespace fast
+
+bool fast_pass_eligible(const PassParams& p, int arith) {
+  fast::FastArgs a;
+  bool ri, ro;
+  return kernel_path() == 1 && p.kpath == 0 && fast::fast_args(p, arith, &a, &ri, &ro);
+}
+
 // Returns -1 when the pass is not covered by the fast kernel.
 int launch_fast_pass(const PassParams& p, int arith, cudaStream_t stream) {
   using namespace fast;
-  if (p.mode != MODE_C2C || p.nst == 0) return -1;
-  if (p.M != p.N || p.Ni != p.N || p.No != p.N || p.Zi || p.Zo || p.wmode) return -1;
-  const int N = p.N;
-  if (N < 64 || N > 4096 || (N & (N - 1))) return -1;
-  if (arith != ARITH_F32 && arith != ARITH_DF) return -1;
-  if (p.ashI.en || p.ashO.en) return -1;
-  for (int b = 0; b < p.nb; b++)
-    if (p.bshI[b].en || p.bshO[b].en) return -1;
-  if (p.nb > PG_MAX_BATCH) return -1;
   FastArgs a;
-  a.src = p.src;
-  a.dst = p.dst;
-  a.tw = p.tw;
-  a.sIa = p.sIa;
-  a.sOa = p.sOa;
-  a.nb = p.nb;
-  for (int b = 0; b < p.nb; b++) {
-    a.bext[b] = p.bext[b];
-    a.bsI[b] = p.bsI[b];
-    a.bsO[b] = p.bsO[b];
-  }
-  a.nlines = p.nlines;
-  a.conj_in = p.conj_in;
-  a.conj_out = p.conj_out;
-  a.in_df = p.in_df;
-  a.out_df = p.out_df;
-  const bool row_in = p.sIa == 1, row_out = p.sOa == 1;
-  // column mapping needs adjacent lines on that side
-  if (!row_in && !(p.nb > 0 && p.bsI[0] == 1)) return -1;
-  if (!row_out && !(p.nb > 0 && p.bsO[0] == 1)) return -1;
+  bool row_in, row_out;
+  if (!fast_args(p, arith, &a, &row_in, &row_out)) return -1;
+  const int N = p.N;
   const bool big = N >= 1024;
+  a.fastL = p.fastL;
   if (arith == ARITH_F32) {
     if (p.sign < 0)
       return big ? launch_large<F32, -1>(N, a, row_in, row_out, stream) : launch_small<F32, -1>(N, a, row_in, row_out, stream);

@@ -179,22 +179,37 @@ struct FastArgs {
   long long nlines;
   int conj_in, conj_out;
   int in_df, out_df;  // double API: the array holds float-float pairs (an intermediate)
+  int fastL;          // requested lines per CTA (0: default); 512 takes 4 or 8, 1024 takes 2 or 4
 };
 
 // global element access: native format, or float-float pairs for the
-// intermediate arrays of the double API (same 16 bytes per complex value)
-template <class P>
+// intermediate arrays of the double API (same 16 bytes per complex value).
+// CG: load through L2 only (data written earlier in the same launch).
+template <bool CG, class T>
+__device__ __forceinline__ T gld(const T* p) {
+  if (CG) return __ldcg(p);
+  return *p;
+}
+template <class P, bool CG>
 __device__ __forceinline__ typename P::C gload(const typename P::G* p, int df);
 template <>
-__device__ __forceinline__ F32::C gload<F32>(const F32::G* p, int) { return *p; }
+__device__ __forceinline__ F32::C gload<F32, false>(const F32::G* p, int) { return *p; }
 template <>
-__device__ __forceinline__ FDD::C gload<FDD>(const FDD::G* p, int df) {
-  if (df) {
-    float4 v = *(const float4*)p;
+__device__ __forceinline__ F32::C gload<F32, true>(const F32::G* p, int) { return __ldcg(p); }
+template <bool CG>
+__device__ __forceinline__ FDD::C gload_fdd(const FDD::G* p, int isdf) {
+  if (isdf) {
+    float4 v = gld<CG>((const float4*)p);
     return {{v.x, v.y}, {v.z, v.w}};
   }
-  return FDD::ld(p);
+  double2 v = gld<CG>(p);
+  df a = df_from_double(v.x), b = df_from_double(v.y);
+  return {{a.hi, a.lo}, {b.hi, b.lo}};
 }
+template <>
+__device__ __forceinline__ FDD::C gload<FDD, false>(const FDD::G* p, int df) { return gload_fdd<false>(p, df); }
+template <>
+__device__ __forceinline__ FDD::C gload<FDD, true>(const FDD::G* p, int df) { return gload_fdd<true>(p, df); }
 template <class P>
 __device__ __forceinline__ void gstore(typename P::G* p, typename P::C v, int df);
 template <>
@@ -215,8 +230,12 @@ __device__ __forceinline__ void gstore<FDD>(FDD::G* p, FDD::C v, int df) {
 // through shared memory so that both sides stay coalesced.
 // Shared memory: one buffer of L lines, line stride N + N/8 + 1 (odd, so the
 // lines of a warp fall on different banks), index p + p/8 within a line.
-template <class P, int SIGN, int N, int L, bool ROW_IN, bool ROW_OUT>
-__global__ void __launch_bounds__(L*(N / 8)) k_fast(const FastArgs a) {
+// One tile (L lines) of the pass, run by the L * N/8 threads of a block:
+// the body of the stand-alone kernel k_fast, and a task of the batched
+// persistent kernel.  `blk` is the tile index, `sm_raw` the block's dynamic
+// shared memory (fast_smem_bytes).
+template <class P, int SIGN, int N, int L, bool ROW_IN, bool ROW_OUT, bool CG = false>
+__device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsigned char* sm_raw) {
   typedef typename P::C C;
   typedef typename P::S S;
   typedef typename P::G G;
@@ -224,13 +243,12 @@ __global__ void __launch_bounds__(L*(N / 8)) k_fast(const FastArgs a) {
   constexpr int NS8 = n8_of(N);
   constexpr int Q = N / pow8(NS8);  // last radix: 1, 2 or 4
   constexpr int LSP = N + N / 8 + 1;
-  extern __shared__ __align__(16) unsigned char sm_raw[];
   long long* offI = (long long*)sm_raw;
   long long* offO = offI + L;
   S* buf = (S*)(sm_raw + 16 * L);
 
   const int tid = threadIdx.x;
-  const long long g0 = (long long)blockIdx.x * L;
+  const long long g0 = blk * L;
   if (tid < L) {
     long long g = g0 + tid;
     if (g >= a.nlines) g = a.nlines - 1;  // tail CTA: clamp (duplicate work, never stored)
@@ -258,7 +276,7 @@ __global__ void __launch_bounds__(L*(N / 8)) k_fast(const FastArgs a) {
     const long long st = (long long)TPL * a.sIa;
 #pragma unroll
     for (int r = 0; r < 8; r++) {
-      v[r] = gload<P>(src + r * st, a.in_df);
+      v[r] = gload<P, CG>(src + r * st, a.in_df);
       if (a.conj_in) v[r] = P::conj(v[r]);
     }
   }
@@ -366,10 +384,21 @@ __global__ void __launch_bounds__(L*(N / 8)) k_fast(const FastArgs a) {
   }
 }
 
+template <class P, int SIGN, int N, int L, bool ROW_IN, bool ROW_OUT>
+__global__ void __launch_bounds__(L*(N / 8)) k_fast(const FastArgs a) {
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  fast_tile<P, SIGN, N, L, ROW_IN, ROW_OUT>(a, blockIdx.x, sm_raw);
+}
+
+template <class P, int N, int L>
+constexpr size_t fast_smem_bytes() {
+  return 16 * L + (size_t)L * (N + N / 8 + 1) * sizeof(typename P::S);
+}
+
 template <class P, int SIGN, int N, int L>
 int launch4(const FastArgs& a, bool row_in, bool row_out, cudaStream_t s) {
   constexpr int T = L * (N / 8);
-  const size_t smem = 16 * L + (size_t)L * (N + N / 8 + 1) * sizeof(typename P::S);
+  const size_t smem = fast_smem_bytes<P, N, L>();
   long long grid = (a.nlines + L - 1) / L;
   if (grid > 2147483647LL) return (int)cudaErrorInvalidConfiguration;
   cudaError_t e = cudaSuccess;
@@ -396,6 +425,10 @@ int launch4(const FastArgs& a, bool row_in, bool row_out, cudaStream_t s) {
 #undef PG_FAST_LAUNCH
   return (int)cudaGetLastError();
 }
+
+// Arguments of the fast kernel for a pass, or false when the pass is not
+// covered (fft_fast.cu).
+bool fast_args(const PassParams& p, int arith, FastArgs* a, bool* row_in, bool* row_out);
 
 // Launchers, one explicit instantiation set per translation unit
 // (fft_fast_<arith>_<dir>_<range>.cu) so the build compiles them in parallel.

@@ -8,7 +8,10 @@ template <class P, int SIGN>
 int launch_large(int N, const FastArgs& a, bool row_in, bool row_out, cudaStream_t s) {
   const bool col = !(row_in && row_out);
   switch (N) {
-    case 1024: return col ? launch4<P, SIGN, 1024, 4>(a, row_in, row_out, s) : launch4<P, SIGN, 1024, 2>(a, row_in, row_out, s);
+    case 1024: {
+      const int L = a.fastL ? a.fastL : (col ? 4 : 2);
+      return L == 4 ? launch4<P, SIGN, 1024, 4>(a, row_in, row_out, s) : launch4<P, SIGN, 1024, 2>(a, row_in, row_out, s);
+    }
     case 2048: return launch4<P, SIGN, 2048, 2>(a, row_in, row_out, s);
     case 4096: return launch4<P, SIGN, 4096, 1>(a, row_in, row_out, s);
   }

@@ -11,7 +11,10 @@ int launch_small(int N, const FastArgs& a, bool row_in, bool row_out, cudaStream
     case 64: return launch4<P, SIGN, 64, 32>(a, row_in, row_out, s);
     case 128: return launch4<P, SIGN, 128, 16>(a, row_in, row_out, s);
     case 256: return launch4<P, SIGN, 256, 8>(a, row_in, row_out, s);
-    case 512: return col ? launch4<P, SIGN, 512, 8>(a, row_in, row_out, s) : launch4<P, SIGN, 512, 4>(a, row_in, row_out, s);
+    case 512: {
+      const int L = a.fastL ? a.fastL : (col ? 8 : 4);
+      return L == 8 ? launch4<P, SIGN, 512, 8>(a, row_in, row_out, s) : launch4<P, SIGN, 512, 4>(a, row_in, row_out, s);
+    }
   }
   return -1;
 }

@@ -43,7 +43,7 @@ int kernel_path() {
 void set_kernel_path(int v) { g_kernel_path = v; }
 
 int launch_pass(const PassParams& p, int arith, cudaStream_t stream) {
-  if (kernel_path() == 1) {
+  if (kernel_path() == 1 && p.kpath == 0) {
     int rc = launch_fast_pass(p, arith, stream);
     if (rc != -1) return rc;
   }

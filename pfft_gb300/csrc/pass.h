@@ -75,12 +75,16 @@ struct PassParams {
   int in_df, out_df;  // double API: complex array held as float-float pairs (intermediates)
   int threads;
   int smem_bytes;
+  int kpath;    // 0: register-resident radix-8 kernel where it applies, 1: general kernel
+  int fastL;    // radix-8 kernel lines per CTA (0: default for the length)
 };
 
 // Launch one pass on `stream`.  Returns a cudaError_t value.
 int launch_pass(const PassParams& p, int arith, cudaStream_t stream);
 // 1: use the register-resident kernel where it applies (default), 0: generic only
 int kernel_path();
+// true when launch_pass runs this pass on the register-resident radix-8 kernel
+bool fast_pass_eligible(const PassParams& p, int arith);
 void set_kernel_path(int v);
 
 // Shared-memory element size of a policy.

@@ -60,11 +60,26 @@ static int g_double_arith = -1;
 int double_arith() {
   if (g_double_arith < 0) {
     const char* e = getenv("PFFT_GB300_F64_ARITH");
-    g_double_arith = (e && strcmp(e, "native") == 0) ? ARITH_F64 : ARITH_DF;
+    g_double_arith = (e && strcmp(e, "native") == 0) ? DARITH_NATIVE
+                     : (e && strcmp(e, "df") == 0)   ? DARITH_DF
+                                                     : DARITH_AUTO;
   }
   return g_double_arith;
 }
 void set_double_arith(int a) { g_double_arith = a; }
+
+// Arithmetic of one double-precision plan.  Native FP64 issues at about 1/64
+// of the FP32 rate on this part, so large transforms run in float-float; a
+// transform of at most DARITH_AUTO_POINTS points costs no more than a launch
+// latency in FP64 and keeps full double rounding.
+int plan_double_arith(const PlanDesc& d) {
+  const int m = double_arith();
+  if (m == DARITH_NATIVE) return ARITH_F64;
+  if (m == DARITH_DF) return ARITH_DF;
+  double pts = (double)d.howmany;
+  for (int t = 0; t < d.rnk_n; t++) pts *= (double)d.n[t];
+  return pts <= (double)DARITH_AUTO_POINTS ? ARITH_F64 : ARITH_DF;
+}
 
 // ---- plans -------------------------------------------------------------------
 bool ensure_workspace(Plan* pl, const PassProgram& prog) {
@@ -123,7 +138,7 @@ static void collect_pass_times(Plan* pl) {
 Plan* make_plan(const PlanDesc& base, void* in, void* out) {
   Plan* pl = new Plan();
   pl->d = base;
-  pl->arith = base.prec == 0 ? ARITH_F32 : double_arith();
+  pl->arith = base.prec == 0 ? ARITH_F32 : plan_double_arith(base);
   pl->in = in;
   pl->out = out;
   pl->inplace = (in == out) && in != nullptr;
@@ -132,6 +147,11 @@ Plan* make_plan(const PlanDesc& base, void* in, void* out) {
     return nullptr;
   }
   if (!ensure_workspace(pl, pl->fwd)) {
+    destroy_plan(pl);
+    return nullptr;
+  }
+  apply_wisdom(&pl->fwd, pl->arith);
+  if ((base.pfft_flags & (F_PATIENT | F_EXHAUSTIVE | F_TUNE)) && !tune_program(pl, &pl->fwd)) {
     destroy_plan(pl);
     return nullptr;
   }
@@ -196,6 +216,8 @@ void execute_plan(Plan* pl, void* in, void* out, bool adjoint) {
       return;
     }
     if (!ensure_workspace(pl, pl->adj)) return;
+    apply_wisdom(&pl->adj, pl->arith);
+    if ((pl->d.pfft_flags & (F_PATIENT | F_EXHAUSTIVE | F_TUNE)) && !tune_program(pl, &pl->adj)) return;
     pl->adj_built = true;
   }
   const PassProgram& prog = adjoint ? pl->adj : pl->fwd;

@@ -59,13 +59,18 @@ long long complex_len(int mode, long long N) {
   return N;
 }
 
-bool factorize(int M, int* radix, int* nst, bool* generic) {
+// Radix schedule of a length-M line.  pref 0: radix 16 first (then one 8, 4
+// or 2), 1: radix 8 first, 2: radix 4 first; then 3, 5, 7, 11, 13 and any
+// larger prime (generic stage).
+bool factorize(int M, int* radix, int* nst, bool* generic, int pref) {
   *nst = 0;
   *generic = false;
   int m = M;
-  while (m % 16 == 0 && m > 8) {
-    radix[(*nst)++] = 16;
-    m /= 16;
+  const int big = pref == 1 ? 8 : (pref == 2 ? 4 : 16);
+  while (m % big == 0 && m > big / 2) {
+    radix[(*nst)++] = big;
+    m /= big;
+    if (*nst >= PG_MAX_STAGES) return false;
   }
   if (m % 8 == 0) {
     radix[(*nst)++] = 8;
@@ -150,6 +155,50 @@ bool mode_cplx_in(int mode) { return mode == MODE_C2C || mode == MODE_C2R; }
 bool mode_cplx_out(int mode) { return mode == MODE_C2C || mode == MODE_R2C; }
 
 }  // namespace
+
+// Re-plan the general kernel of a pass with radix order `pref` and `L`
+// lines per CTA (0: keep).  Returns false when the shape does not fit one CTA
+// (512 threads, 200 KB of shared memory); the pass is then unchanged.
+bool refit_pass(PassParams* p, int arith, int pref, int L) {
+  if (p->nst == 0) return L <= 0 || L == p->L;
+  PassParams q = *p;
+  bool generic = false;
+  if (!factorize(q.M, q.radix, &q.nst, &generic, pref)) return false;
+  q.pingpong = generic ? 1 : 0;
+  if (L > 0) q.L = (int)std::min<long long>(L, std::max(1LL, q.nlines));
+  int T = 64;
+  for (int st = 0; st < q.nst; st++) T = std::max(T, stage_threads(q.radix[st], (long long)q.L * q.M));
+  T = (T + 31) / 32 * 32;
+  if (T > 512) return false;
+  long long meta = ((2 * 8 + 2 * 4) * (long long)q.L + 15) & ~15LL;
+  long long smem = meta + (long long)q.L * q.LS * arith_sm_bytes(arith) * (q.pingpong ? 2 : 1);
+  if (smem > 200 * 1024) return false;
+  q.threads = T;
+  q.smem_bytes = (int)smem;
+  *p = q;
+  return true;
+}
+
+// Re-fit a general pass to at most max_threads threads per CTA (the
+// batched persistent launch runs every tile with one block size): halve the
+// lines per tile until every register stage's butterflies are covered.
+bool fit_pass_threads(PassParams* p, int arith, int max_threads) {
+  long long L = p->L;
+  for (;;) {
+    int T = 32;
+    for (int st = 0; st < p->nst; st++) T = std::max(T, stage_threads(p->radix[st], L * p->M));
+    T = (T + 31) / 32 * 32;
+    if (T <= max_threads) {
+      p->L = (int)L;
+      p->threads = T;
+      long long meta = ((2 * 8 + 2 * 4) * L + 15) & ~15LL;
+      p->smem_bytes = (int)(meta + L * p->LS * (long long)arith_sm_bytes(arith) * (p->pingpong ? 2 : 1));
+      return true;
+    }
+    if (L == 1) return false;
+    L = std::max(1LL, L / 2);
+  }
+}
 
 bool build_program(const PlanDesc& d, int arith, bool inplace, bool adjoint, PassProgram* prog) {
   const int D = d.rnk_n;
@@ -431,7 +480,7 @@ bool build_program(const PlanDesc& d, int arith, bool inplace, bool adjoint, Pas
     bool generic = false;
     if (s.identity) {
       p.nst = 0;
-    } else if (!factorize(s.M, p.radix, &p.nst, &generic)) {
+    } else if (!factorize(s.M, p.radix, &p.nst, &generic, 0)) {
       set_error(7, "transform length has too many factors");
       return false;
     }

@@ -83,15 +83,43 @@ def comm_for(req):
     return pg.MPI_COMM_WORLD if req.cart == 0 else pg.procmesh(req.cart)
 
 
+class double_arith:
+    """Context manager selecting the double API's arithmetic for the plans
+    created inside it: "double" keeps the default (by size), "double-df" forces
+    float-float, "double-f64" native FP64; "float" changes nothing."""
+
+    MODES = {"double-df": 0, "double-f64": 1}
+
+    def __init__(self, prec):
+        self.mode = self.MODES.get(prec)
+
+    def __enter__(self):
+        if self.mode is not None:
+            L = pg.lib()
+            self.old = L.pfft_gb300_get_double_arith()
+            assert L.pfft_gb300_set_double_arith(self.mode) == 0
+        return self
+
+    def __exit__(self, *exc):
+        if self.mode is not None:
+            pg.lib().pfft_gb300_set_double_arith(self.old)
+        return False
+
+
+def is_double(prec):
+    return prec != "float"
+
+
 def gpu_run(req, x, prec="double", inplace=False, adjoint=False, torch=None, keep=False):
     """Plan + execute through the C-ABI with device arrays; returns float64
     numpy of the output layout (the adjoint maps the output layout to the
-    input layout)."""
+    input layout).  prec: "float", "double" (default arithmetic), "double-df"
+    or "double-f64"."""
     import torch as _t
     torch = torch or _t
     L = pg.lib()
-    pre = "pfft_" if prec == "double" else "pfftf_"
-    rdt = torch.float64 if prec == "double" else torch.float32
+    pre = "pfft_" if is_double(prec) else "pfftf_"
+    rdt = torch.float64 if is_double(prec) else torch.float32
     ci, co, mem = req.counts()
     words = 2 * mem  # alloc_local is in complex units for complex arrays
     words = max(words, ci, co)
@@ -104,11 +132,13 @@ def gpu_run(req, x, prec="double", inplace=False, adjoint=False, torch=None, kee
     comm = comm_for(req)
     fn = getattr(L, pre + PLAN_NAME[req.kind])
     n, ni, no = pg.ints(req.n), pg.ints(req.ni), pg.ints(req.no)
-    if req.kind == "r2r":
-        kinds = pg.cints(req.kinds)
-        plan = fn(req.d, n, ni, no, req.howmany, None, None, a.data_ptr(), b.data_ptr(), comm, kinds, req.flags)
-    else:
-        plan = fn(req.d, n, ni, no, req.howmany, None, None, a.data_ptr(), b.data_ptr(), comm, req.sign, req.flags)
+    with double_arith(prec):
+        if req.kind == "r2r":
+            kinds = pg.cints(req.kinds)
+            plan = fn(req.d, n, ni, no, req.howmany, None, None, a.data_ptr(), b.data_ptr(), comm, kinds, req.flags)
+        else:
+            plan = fn(req.d, n, ni, no, req.howmany, None, None, a.data_ptr(), b.data_ptr(), comm, req.sign,
+                      req.flags)
     if not plan:
         raise RuntimeError("planner returned NULL: %s" % (pg.last_error(),))
     try:

@@ -38,7 +38,7 @@ CASES = [
 
 
 @pytest.mark.parametrize("req", CASES, ids=lambda r: "%s-%s-%x" % (r.kind, "x".join(map(str, r.n)), r.flags))
-@pytest.mark.parametrize("prec,tol", [("double", 1e-12), ("float", 2e-6)])
+@pytest.mark.parametrize("prec,tol", [("double", 1e-12), ("double-df", 1e-12), ("float", 2e-6)])
 def test_dot_product_identity(cuda, pfft_lib, req, prec, tol):
     rng = np.random.default_rng(5)
     x = _mask_in_padding(req, random_input(req, rng))
@@ -66,7 +66,8 @@ def _weights_c2r_input(n_last_logical, half):
     return w
 
 
-def test_r2c_adjoint_matches_reference_gradient(cuda, pfft_lib):
+@pytest.mark.parametrize("prec", ["double", "double-df"])
+def test_r2c_adjoint_matches_reference_gradient(cuda, pfft_lib, prec):
     """Adjoint of an oversampled r2c = the reference's c2r plan (n -> ni)
     applied to the Hermitian-weighted half spectrum, then truncation."""
     n, ni = (32, 30, 28), (16, 15, 14)
@@ -74,7 +75,7 @@ def test_r2c_adjoint_matches_reference_gradient(cuda, pfft_lib):
     rng = np.random.default_rng(6)
     _, co, _ = req.counts()
     g = rng.uniform(-1, 1, co)
-    got = gpu_run(req, g, prec="double", adjoint=True)
+    got = gpu_run(req, g, prec=prec, adjoint=True)
     h = n[2] // 2 + 1
     gw = g.view(np.complex128).reshape(n[0], n[1], h) * _weights_c2r_input(n[2], h)
     ref_req = Req("c2r", n, no=ni, sign=1)

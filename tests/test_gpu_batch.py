@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 import pfft_gb300 as pg
-from tests.pfft_util import Req, oracle_run, rel_l2
+from tests.pfft_util import Req, double_arith, oracle_run, rel_l2
 
 pytestmark = pytest.mark.gpu
 
@@ -21,8 +21,8 @@ SIZES = [(32, 32, 32), (48, 64, 40), (96, 96, 96), (128, 128, 64), (128, 128, 12
 
 def make_plans(torch, prec, count, seed, flags=0):
     L = pg.lib()
-    pre = "pfft_" if prec == "double" else "pfftf_"
-    cdt = torch.complex128 if prec == "double" else torch.complex64
+    pre = "pfftf_" if prec == "float" else "pfft_"
+    cdt = torch.complex64 if prec == "float" else torch.complex128
     rng = np.random.default_rng(seed)
     comm = pg.procmesh(2)
     plans, arrays = [], []
@@ -31,14 +31,15 @@ def make_plans(torch, prec, count, seed, flags=0):
         x = rng.uniform(-1, 1, 2 * int(np.prod(n)))
         a = torch.from_numpy(x).view(torch.complex128).to(cdt).cuda()
         b = torch.zeros_like(a)
-        p = getattr(L, pre + "plan_dft_3d")(pg.ints(n), a.data_ptr(), b.data_ptr(), comm, -1, flags)
+        with double_arith(prec):
+            p = getattr(L, pre + "plan_dft_3d")(pg.ints(n), a.data_ptr(), b.data_ptr(), comm, -1, flags)
         assert p
         plans.append(p)
         arrays.append((n, x, a, b))
     return pre, plans, arrays
 
 
-@pytest.mark.parametrize("prec,tol", [("double", 1e-12), ("float", 2e-6)])
+@pytest.mark.parametrize("prec,tol", [("double", 1e-12), ("double-df", 1e-12), ("float", 2e-6)])
 def test_batch_matches_oracle(cuda, pfft_lib, prec, tol):
     torch = cuda
     L = pg.lib()
@@ -53,7 +54,7 @@ def test_batch_matches_oracle(cuda, pfft_lib, prec, tol):
             torch.cuda.synchronize()
             assert L.pfft_gb300_batch_execute(b) == 0
             for (n, x, a, out) in arrays:
-                xin = x if prec == "double" else x.astype(np.float32).astype(np.float64)
+                xin = x.astype(np.float32).astype(np.float64) if prec == "float" else x
                 ref = oracle_run(Req("c2c", n, flags=pg.PFFT_TRANSPOSED_OUT), xin)
                 got = torch.view_as_real(out).double().cpu().numpy().ravel()
                 assert rel_l2(got, ref) <= tol

@@ -5,7 +5,10 @@ sizes (29x27x31, 13x14x19x17, 2x2x4, 16^3 <-> 29x27x31 oversampling),
 transposed layouts, in-place and out-of-place arrays, r2c/c2r padding, the
 r2r kinds they use, plus the configurations of the benchmark suite at sizes
 the oracle finishes in seconds.  Tolerances: relative L2 <= 1e-12 for the
-double API, <= 2e-6 for the float API.
+double API, <= 2e-6 for the float API.  The double API is run with its
+default arithmetic ("double": native FP64 up to 2^18 points, float-float
+above) and with float-float forced ("double-df"), so both arithmetics are
+checked at every size.
 """
 import numpy as np
 import pytest
@@ -15,7 +18,9 @@ from tests.pfft_util import Req, gpu_run, mask_padding, oracle_run, random_input
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"double": 1e-12, "float": 2e-6}
+TOL = {"double": 1e-12, "double-df": 1e-12, "double-f64": 1e-12, "float": 2e-6}
+PRECS = ["double", "double-df", "float"]
+DPRECS = ["double", "double-df"]
 TO, TI = pg.PFFT_TRANSPOSED_OUT, pg.PFFT_TRANSPOSED_IN
 PAD = pg.PFFT_PADDED_R2C
 
@@ -40,111 +45,125 @@ C2C_CASES = [
 
 
 @pytest.mark.parametrize("n,flags", C2C_CASES)
-@pytest.mark.parametrize("prec", ["double", "float"])
+@pytest.mark.parametrize("prec", PRECS)
 def test_c2c_3d(cuda, pfft_lib, n, flags, prec):
     check(Req("c2c", n, flags=flags), prec)
 
 
 @pytest.mark.parametrize("sign", [-1, 1])
-def test_c2c_backward_and_inplace(cuda, pfft_lib, sign):
-    check(Req("c2c", (29, 27, 31), sign=sign), inplace=True)
-    check(Req("c2c", (29, 27, 31), sign=sign, flags=TO), inplace=True)
+@pytest.mark.parametrize("prec", ["double", "double-df"])
+def test_c2c_backward_and_inplace(cuda, pfft_lib, sign, prec):
+    check(Req("c2c", (29, 27, 31), sign=sign), prec, inplace=True)
+    check(Req("c2c", (29, 27, 31), sign=sign, flags=TO), prec, inplace=True)
 
 
 @pytest.mark.parametrize("n,flags", [((8, 8, 8), 0), ((29, 27, 31), 0), ((16, 16, 16), TO), ((29, 27, 31), TO),
                                      ((16, 16, 16), PAD), ((29, 27, 31), PAD | TO), ((64, 64, 64), PAD | TO)])
-@pytest.mark.parametrize("prec", ["double", "float"])
+@pytest.mark.parametrize("prec", PRECS)
 def test_r2c(cuda, pfft_lib, n, flags, prec):
     check(Req("r2c", n, flags=flags), prec, dist="normal")
 
 
 @pytest.mark.parametrize("n,flags", [((8, 8, 8), 0), ((29, 27, 31), 0), ((16, 16, 16), TI), ((29, 27, 31), TI),
                                      ((16, 16, 16), PAD), ((29, 27, 31), PAD | TI), ((64, 64, 64), PAD | TI)])
-@pytest.mark.parametrize("prec", ["double", "float"])
+@pytest.mark.parametrize("prec", PRECS)
 def test_c2r(cuda, pfft_lib, n, flags, prec):
     check(Req("c2r", n, sign=1, flags=flags), prec)
 
 
-def test_r2c_backward_c2r_forward(cuda, pfft_lib):
+@pytest.mark.parametrize("prec", DPRECS)
+def test_r2c_backward_c2r_forward(cuda, pfft_lib, prec):
     # conjugation paths (kernel/partrafo.c:428-443)
-    check(Req("r2c", (12, 10, 16), sign=1), dist="normal")
-    check(Req("c2r", (12, 10, 16), sign=-1))
+    check(Req("r2c", (12, 10, 16), sign=1), prec, dist="normal")
+    check(Req("c2r", (12, 10, 16), sign=-1), prec)
 
 
-def test_r2c_c2r_inplace_padded(cuda, pfft_lib):
-    check(Req("r2c", (16, 12, 10), flags=PAD), inplace=True, dist="normal")
-    check(Req("c2r", (16, 12, 10), sign=1, flags=PAD), inplace=True)
-    check(Req("r2c", (16, 12, 10), flags=PAD | TO), inplace=True, dist="normal")
-    check(Req("c2r", (16, 12, 10), sign=1, flags=PAD | TI), inplace=True)
+@pytest.mark.parametrize("prec", DPRECS)
+def test_r2c_c2r_inplace_padded(cuda, pfft_lib, prec):
+    check(Req("r2c", (16, 12, 10), flags=PAD), prec, inplace=True, dist="normal")
+    check(Req("c2r", (16, 12, 10), sign=1, flags=PAD), prec, inplace=True)
+    check(Req("r2c", (16, 12, 10), flags=PAD | TO), prec, inplace=True, dist="normal")
+    check(Req("c2r", (16, 12, 10), sign=1, flags=PAD | TI), prec, inplace=True)
 
 
 @pytest.mark.parametrize("kinds", [(3, 3, 3), (4, 4, 4), (5, 5, 5), (6, 6, 6), (7, 7, 7), (8, 8, 8), (9, 9, 9),
                                    (10, 10, 10), (0, 1, 2), (3, 4, 7), (5, 9, 6)])
-@pytest.mark.parametrize("prec", ["double", "float"])
+@pytest.mark.parametrize("prec", PRECS)
 def test_r2r(cuda, pfft_lib, kinds, prec):
     check(Req("r2r", (9, 8, 10), kinds=list(kinds)), prec, dist="normal")
 
 
-def test_r2r_transposed(cuda, pfft_lib):
-    check(Req("r2r", (16, 16, 16), kinds=[5, 5, 5], flags=TO), dist="normal")
-    check(Req("r2r", (16, 16, 16), kinds=[4, 4, 4], flags=TI), dist="normal")
+@pytest.mark.parametrize("prec", DPRECS)
+def test_r2r_transposed(cuda, pfft_lib, prec):
+    check(Req("r2r", (16, 16, 16), kinds=[5, 5, 5], flags=TO), prec, dist="normal")
+    check(Req("r2r", (16, 16, 16), kinds=[4, 4, 4], flags=TI), prec, dist="normal")
 
 
-def test_ousam_c2c(cuda, pfft_lib):
+@pytest.mark.parametrize("prec", DPRECS)
+def test_ousam_c2c(cuda, pfft_lib, prec):
     # tests/simple_check_ousam_c2c.c: ni = 16^3 -> n = 29x27x31 -> no = n, and back
-    check(Req("c2c", (29, 27, 31), ni=(16, 16, 16)))
-    check(Req("c2c", (29, 27, 31), no=(16, 16, 16), sign=1))
-    check(Req("c2c", (29, 27, 31), ni=(16, 16, 16), no=(20, 18, 16), flags=TO))
+    check(Req("c2c", (29, 27, 31), ni=(16, 16, 16)), prec)
+    check(Req("c2c", (29, 27, 31), no=(16, 16, 16), sign=1), prec)
+    check(Req("c2c", (29, 27, 31), ni=(16, 16, 16), no=(20, 18, 16), flags=TO), prec)
 
 
-def test_ousam_r2c_c2r(cuda, pfft_lib):
-    check(Req("r2c", (29, 27, 31), ni=(16, 16, 16)), dist="normal")
-    check(Req("c2r", (29, 27, 31), no=(16, 16, 16), sign=1))
-    check(Req("r2c", (32, 32, 32), ni=(16, 16, 16), flags=PAD | TO), dist="normal")
+@pytest.mark.parametrize("prec", DPRECS)
+def test_ousam_r2c_c2r(cuda, pfft_lib, prec):
+    check(Req("r2c", (29, 27, 31), ni=(16, 16, 16)), prec, dist="normal")
+    check(Req("c2r", (29, 27, 31), no=(16, 16, 16), sign=1), prec)
+    check(Req("r2c", (32, 32, 32), ni=(16, 16, 16), flags=PAD | TO), prec, dist="normal")
     # truncated r2c output keeps the reference's bin range
-    check(Req("r2c", (32, 30, 28), no=(16, 16, 16)), dist="normal")
+    check(Req("r2c", (32, 30, 28), no=(16, 16, 16)), prec, dist="normal")
 
 
-def test_shifted(cuda, pfft_lib):
+@pytest.mark.parametrize("prec", DPRECS)
+def test_shifted(cuda, pfft_lib, prec):
     S_IN, S_OUT = pg.PFFT_SHIFTED_IN, pg.PFFT_SHIFTED_OUT
-    check(Req("c2c", (8, 10, 12), flags=S_IN | S_OUT))
-    check(Req("c2c", (8, 10, 12), flags=S_OUT))
-    check(Req("c2c", (8, 10, 12), flags=S_IN))
-    check(Req("c2c", (16, 16, 16), ni=(8, 8, 8), flags=S_IN | S_OUT))
-    check(Req("r2c", (8, 10, 12), flags=S_IN | S_OUT), dist="normal")
+    check(Req("c2c", (8, 10, 12), flags=S_IN | S_OUT), prec)
+    check(Req("c2c", (8, 10, 12), flags=S_OUT), prec)
+    check(Req("c2c", (8, 10, 12), flags=S_IN), prec)
+    check(Req("c2c", (16, 16, 16), ni=(8, 8, 8), flags=S_IN | S_OUT), prec)
+    check(Req("r2c", (8, 10, 12), flags=S_IN | S_OUT), prec, dist="normal")
 
 
-def test_4d_and_meshes(cuda, pfft_lib):
-    check(Req("c2c", (13, 14, 19, 17)))
-    check(Req("c2c", (13, 14, 19, 17), flags=TO))
-    check(Req("c2c", (8, 6, 10, 4), cart=3))
-    check(Req("c2c", (8, 6, 10, 4), cart=3, flags=TO))
-    check(Req("c2c", (12, 10, 8), cart=1, flags=TO))
-    check(Req("c2c", (12, 10, 8), cart=0, flags=TO))
-    check(Req("c2c", (12, 10, 8), cart=3, flags=TO))
-    check(Req("r2c", (12, 10, 8), cart=3, flags=PAD), dist="normal")
+@pytest.mark.parametrize("prec", DPRECS)
+def test_4d_and_meshes(cuda, pfft_lib, prec):
+    check(Req("c2c", (13, 14, 19, 17)), prec)
+    check(Req("c2c", (13, 14, 19, 17), flags=TO), prec)
+    check(Req("c2c", (8, 6, 10, 4), cart=3), prec)
+    check(Req("c2c", (8, 6, 10, 4), cart=3, flags=TO), prec)
+    check(Req("c2c", (12, 10, 8), cart=1, flags=TO), prec)
+    check(Req("c2c", (12, 10, 8), cart=0, flags=TO), prec)
+    check(Req("c2c", (12, 10, 8), cart=3, flags=TO), prec)
+    check(Req("r2c", (12, 10, 8), cart=3, flags=PAD), prec, dist="normal")
 
 
-def test_howmany(cuda, pfft_lib):
-    check(Req("c2c", (8, 8, 8), howmany=2))
-    check(Req("c2c", (8, 8, 8), howmany=3, flags=TO))
-    check(Req("r2c", (8, 8, 8), howmany=2), dist="normal")
-    check(Req("c2r", (8, 8, 8), howmany=2, sign=1))
+@pytest.mark.parametrize("prec", DPRECS)
+def test_howmany(cuda, pfft_lib, prec):
+    check(Req("c2c", (8, 8, 8), howmany=2), prec)
+    check(Req("c2c", (8, 8, 8), howmany=3, flags=TO), prec)
+    check(Req("r2c", (8, 8, 8), howmany=2), prec, dist="normal")
+    check(Req("c2r", (8, 8, 8), howmany=2, sign=1), prec)
 
 
 def test_native_f64_arith(cuda, pfft_lib):
+    check(Req("c2c", (29, 27, 31), flags=TO), "double-f64")
+    check(Req("r2c", (16, 16, 16), flags=PAD), "double-f64", dist="normal")
+    check(Req("c2c", (128, 64, 256), flags=TO), "double-f64")
+
+
+def test_double_arith_modes(cuda, pfft_lib):
+    """Mode selection: unknown modes are refused, the previous mode stays."""
     L = pg.lib()
-    L.pfft_gb300_set_double_arith(1)
-    try:
-        check(Req("c2c", (29, 27, 31), flags=TO))
-        check(Req("r2c", (16, 16, 16), flags=PAD), dist="normal")
-    finally:
-        L.pfft_gb300_set_double_arith(0)
+    old = L.pfft_gb300_get_double_arith()
+    assert old in (0, 1, 2)
+    assert L.pfft_gb300_set_double_arith(7) == -1
+    assert L.pfft_gb300_get_double_arith() == old
 
 
 @pytest.mark.parametrize("n,flags", [((64, 64, 64), 0), ((128, 64, 256), TO), ((512, 8, 16), 0),
                                      ((16, 1024, 8), TI), ((2048, 4, 4), 0), ((8, 4, 4096), 0)])
-@pytest.mark.parametrize("prec", ["double", "float"])
+@pytest.mark.parametrize("prec", PRECS)
 def test_kernel_paths_agree(cuda, pfft_lib, n, flags, prec):
     """The register-resident radix-8 kernel and the general pass kernel both
     match the oracle on power-of-two c2c lines (row, column and transposing
