@@ -327,6 +327,7 @@ def main():
     ap.add_argument("--ref-sample-n0", type=int, default=128)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--n", type=int, default=512, help="cube edge (profiling runs use a smaller case)")
+    ap.add_argument("--shape", default=None, help="n0xn1xn2 instead of a cube (profiling runs)")
     ap.add_argument("--prec", default="double", choices=["double", "float"],
                     help="double = pfft_ (complex128, the headline); float = pfftf_ (complex64)")
     args = ap.parse_args()
@@ -341,7 +342,7 @@ def main():
     torch.cuda.set_device(local)
     L = pg.lib()
     dev = torch.device("cuda", local)
-    n = (args.n, args.n, args.n)
+    n = tuple(int(v) for v in args.shape.split("x")) if args.shape else (args.n, args.n, args.n)
     cnt = int(np.prod(n))
     rng = np.random.default_rng(1 + rank)
     host = torch.from_numpy(rng.uniform(-1.0, 1.0, 2 * cnt))
@@ -444,10 +445,12 @@ def main():
         "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": {0: "f32", 1: "f64", 2: "f64 storage, float-float arithmetic"}[plan_arith],
         "data": "synthetic uniform[-1,1) seed 1+rank",
-        "config": {"workload": "pfft_execute c2c %d^3 %s forward, 1x1 procmesh, out-of-place, "
-                               "TRANSPOSED_NONE" % (args.n, "complex128" if args.prec == "double" else "complex64"),
+        "config": {"workload": "pfft_execute c2c %s %s forward, 1x1 procmesh, out-of-place, "
+                               "TRANSPOSED_NONE" % ("x".join(map(str, n)) if args.shape else "%d^3" % args.n,
+                                                    "complex128" if args.prec == "double" else "complex64"),
                    "bytes_per_step": B, "p_min": pmin,
-                   "l2": "arrays (2.1 GB) larger than L2; no flush", "parallelism": "replicas" if world > 1
+                   "l2": "arrays (%.2f GB each) larger than the 129 MB L2; no flush" % (cnt * esz / 1e9),
+                   "parallelism": "replicas" if world > 1
                    else "single GPU"},
         "pct_roofline": value / world / peak,
         "gflops": gflops,

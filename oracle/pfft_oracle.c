@@ -26,7 +26,8 @@
  * of the Hermitian extension (imaginary parts of DC / Nyquist ignored), and
  * the eleven r2r kinds R2HC..RODFT11.  c2c/r2c/c2r use a recursive
  * mixed-radix FFT (Bluestein for large prime lengths); r2r is evaluated
- * directly from its definition.  Twiddles come from long double sin/cos.
+ * directly from its definition, accumulated in double.  Twiddles and the r2r
+ * trigonometric tables come from long double sin/cos.
  *
  * Pinning: the oracle is checked (tests/test_oracle.py) against the
  * reference's own checks - the round trips of tests/simple_check_*.c on the
@@ -235,67 +236,102 @@ static long work_len(const fplan *P) {
 /* ------------------------------------------------------------------------ */
 enum { K_R2HC = 0, K_HC2R, K_DHT, K_RE00, K_RE01, K_RE10, K_RE11, K_RO00, K_RO01, K_RO10, K_RO11 };
 
-/* cos / sin of pi * num / den via an integer-reduced angle */
-static double cospi_frac(long num, long den) {
-  long two = 2 * den;
-  long r = num % two;
-  if (r < 0) r += two;
-  return (double)cosl(3.141592653589793238462643383279502884L * (long double)r / (long double)den);
-}
-static double sinpi_frac(long num, long den) {
-  long two = 2 * den;
-  long r = num % two;
-  if (r < 0) r += two;
-  return (double)sinl(3.141592653589793238462643383279502884L * (long double)r / (long double)den);
+/* cos / sin of pi * m / den for m < 2 den, from long double sin/cos once per
+ * transformed axis (the r2r definitions need angles pi * num / den only) */
+typedef struct {
+  long den;
+  double *c, *s;
+} trig_tab;
+
+static long r2r_den(long n, int kind) {
+  switch (kind) {
+    case K_RE00: return n - 1 > 0 ? n - 1 : 1;
+    case K_RO00: return n + 1;
+    case K_RE01: case K_RE10: case K_RO01: case K_RO10: return 2 * n;
+    case K_RE11: case K_RO11: return 4 * n;
+    default: return n; /* R2HC, HC2R, DHT: angles 2 pi j k / n */
+  }
 }
 
-static void r2r_line(const double *x, double *y, long n, int kind) {
+static void trig_make(trig_tab *t, long den) {
+  t->den = den;
+  t->c = (double *)malloc(sizeof(double) * 2 * (size_t)den);
+  t->s = (double *)malloc(sizeof(double) * 2 * (size_t)den);
+  for (long m = 0; m < 2 * den; m++) {
+    long double a = 3.141592653589793238462643383279502884L * (long double)m / (long double)den;
+    t->c[m] = (double)cosl(a);
+    t->s[m] = (double)sinl(a);
+  }
+}
+
+static void trig_free(trig_tab *t) {
+  free(t->c);
+  free(t->s);
+}
+
+static double cospi_frac(const trig_tab *t, long num) {
+  long two = 2 * t->den;
+  long r = num % two;
+  if (r < 0) r += two;
+  return t->c[r];
+}
+static double sinpi_frac(const trig_tab *t, long num) {
+  long two = 2 * t->den;
+  long r = num % two;
+  if (r < 0) r += two;
+  return t->s[r];
+}
+
+/* One line of a real-to-real transform, by direct evaluation of FFTW's
+ * definitions (doc of FFTW 3.3, "What FFTW Really Computes"), accumulated in
+ * double.  t: the table of trig_make(r2r_den(n, kind)). */
+static void r2r_line(const double *x, double *y, long n, int kind, const trig_tab *t) {
   for (long k = 0; k < n; k++) {
-    long double acc = 0;
+    double acc = 0;
     switch (kind) {
       case K_RE00:
         acc = x[0] + ((k & 1) ? -x[n - 1] : x[n - 1]);
-        for (long j = 1; j < n - 1; j++) acc += 2.0L * x[j] * cospi_frac(j * k, n - 1);
+        for (long j = 1; j < n - 1; j++) acc += 2.0 * x[j] * cospi_frac(t, j * k);
         break;
       case K_RE01:
         acc = x[0];
-        for (long j = 1; j < n; j++) acc += 2.0L * x[j] * cospi_frac(j * (2 * k + 1), 2 * n);
+        for (long j = 1; j < n; j++) acc += 2.0 * x[j] * cospi_frac(t, j * (2 * k + 1));
         break;
       case K_RE10:
-        for (long j = 0; j < n; j++) acc += 2.0L * x[j] * cospi_frac((2 * j + 1) * k, 2 * n);
+        for (long j = 0; j < n; j++) acc += 2.0 * x[j] * cospi_frac(t, (2 * j + 1) * k);
         break;
       case K_RE11:
-        for (long j = 0; j < n; j++) acc += 2.0L * x[j] * cospi_frac((2 * j + 1) * (2 * k + 1), 4 * n);
+        for (long j = 0; j < n; j++) acc += 2.0 * x[j] * cospi_frac(t, (2 * j + 1) * (2 * k + 1));
         break;
       case K_RO00:
-        for (long j = 0; j < n; j++) acc += 2.0L * x[j] * sinpi_frac((j + 1) * (k + 1), n + 1);
+        for (long j = 0; j < n; j++) acc += 2.0 * x[j] * sinpi_frac(t, (j + 1) * (k + 1));
         break;
       case K_RO01:
         acc = (k & 1) ? -x[n - 1] : x[n - 1];
-        for (long j = 0; j < n - 1; j++) acc += 2.0L * x[j] * sinpi_frac((j + 1) * (2 * k + 1), 2 * n);
+        for (long j = 0; j < n - 1; j++) acc += 2.0 * x[j] * sinpi_frac(t, (j + 1) * (2 * k + 1));
         break;
       case K_RO10:
-        for (long j = 0; j < n; j++) acc += 2.0L * x[j] * sinpi_frac((2 * j + 1) * (k + 1), 2 * n);
+        for (long j = 0; j < n; j++) acc += 2.0 * x[j] * sinpi_frac(t, (2 * j + 1) * (k + 1));
         break;
       case K_RO11:
-        for (long j = 0; j < n; j++) acc += 2.0L * x[j] * sinpi_frac((2 * j + 1) * (2 * k + 1), 4 * n);
+        for (long j = 0; j < n; j++) acc += 2.0 * x[j] * sinpi_frac(t, (2 * j + 1) * (2 * k + 1));
         break;
       case K_R2HC:
         if (2 * k <= n) {
-          for (long j = 0; j < n; j++) acc += x[j] * cospi_frac(2 * j * k, n);
+          for (long j = 0; j < n; j++) acc += x[j] * cospi_frac(t, 2 * j * k);
         } else {
           long kk = n - k;
-          for (long j = 0; j < n; j++) acc -= x[j] * sinpi_frac(2 * j * kk, n);
+          for (long j = 0; j < n; j++) acc -= x[j] * sinpi_frac(t, 2 * j * kk);
         }
         break;
       case K_HC2R:
         acc = x[0];
         for (long j = 1; 2 * j < n; j++)
-          acc += 2.0L * (x[j] * cospi_frac(2 * j * k, n) - x[n - j] * sinpi_frac(2 * j * k, n));
-        if (n % 2 == 0) acc += x[n / 2] * ((k & 1) ? -1.0L : 1.0L);
+          acc += 2.0 * (x[j] * cospi_frac(t, 2 * j * k) - x[n - j] * sinpi_frac(t, 2 * j * k));
+        if (n % 2 == 0) acc += x[n / 2] * ((k & 1) ? -1.0 : 1.0);
         break;
       case K_DHT:
-        for (long j = 0; j < n; j++) acc += x[j] * (cospi_frac(2 * j * k, n) + sinpi_frac(2 * j * k, n));
+        for (long j = 0; j < n; j++) acc += x[j] * (cospi_frac(t, 2 * j * k) + sinpi_frac(t, 2 * j * k));
         break;
     }
     y[k] = (double)acc;
@@ -326,6 +362,7 @@ typedef struct {
   long N, Ni, Zi, No, Zo;
   int skip;
   const fplan *P;
+  const trig_tab *T; /* r2r kinds */
   const arr *src;
   arr *dst;
   long nlines;
@@ -398,7 +435,7 @@ static void *axis_worker(void *arg) {
       if (J->skip)
         memcpy(ro, rl, sizeof(double) * (size_t)N);
       else
-        r2r_line(rl, ro, N, kind - 3);
+        r2r_line(rl, ro, N, kind - 3, J->T);
       for (long q = 0; q < J->No; q++) dp[ofs_d + q * inner_d] = ro[J->Zo + q];
     }
   }
@@ -413,13 +450,15 @@ static void axis_transform(const arr *A, arr *B, int axis, int kind, int sign, l
                            long Zo, int skip, int nthreads) {
   long nlines = arr_count(A) / A->ext[axis];
   fplan *P = (kind <= 2) ? fplan_make(N) : NULL;
+  trig_tab T = {0, NULL, NULL};
+  if (kind > 2 && !skip) trig_make(&T, r2r_den(N, kind - 3));
   if (nthreads < 1) nthreads = 1;
   if (nthreads > 256) nthreads = 256;
   if (nlines < nthreads) nthreads = (int)(nlines > 0 ? nlines : 1);
   pthread_t th[256];
   axjob jobs[256];
   for (int i = 0; i < nthreads; i++) {
-    axjob J = {axis, kind, sign, N, Ni, Zi, No, Zo, skip, P, A, B, nlines, nlines * i / nthreads,
+    axjob J = {axis, kind, sign, N, Ni, Zi, No, Zo, skip, P, &T, A, B, nlines, nlines * i / nthreads,
                nlines * (i + 1) / nthreads};
     jobs[i] = J;
   }
@@ -430,6 +469,7 @@ static void axis_transform(const arr *A, arr *B, int axis, int kind, int sign, l
     for (int i = 0; i < nthreads; i++) pthread_join(th[i], NULL);
   }
   fplan_free(P);
+  if (T.c) trig_free(&T);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -631,6 +671,9 @@ int oracle_fft_lines(long n, long nlines, int sign, double *data) {
 }
 
 int oracle_r2r_line(long n, int kind, const double *x, double *y) {
-  r2r_line(x, y, n, kind);
+  trig_tab t;
+  trig_make(&t, r2r_den(n, kind));
+  r2r_line(x, y, n, kind, &t);
+  trig_free(&t);
   return 0;
 }

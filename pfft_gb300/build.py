@@ -48,7 +48,7 @@ def _compile(src, extra):
     if _rdc(src):
         extra = list(extra) + ["-rdc=true"]
     if os.path.basename(src).startswith("batch_tiles"):
-        extra = list(extra) + ["-maxrregcount=128"]  # callees of a kernel bounded to two 256-thread blocks per SM
+        extra = list(extra) + ["-maxrregcount=80"]  # callees of a kernel bounded to three 256-thread blocks per SM
     newest_dep = max([os.path.getmtime(src)] + [os.path.getmtime(h) for h in _headers()])
     if os.path.exists(obj) and os.path.getmtime(obj) >= newest_dep:
         return obj, None

@@ -111,7 +111,11 @@ Batch* make_batch(Plan* const* plans, int n) {
         b->fast_passes++;
       } else {
         bp.fastN = 0;
-        if (!fit_pass_threads(&bp.p, pl->arith, BATCH_THREADS)) {
+        // the batch gets its parallelism from its many plans: start from the
+        // largest tile (64 lines) and halve until it fits the block (256
+        // threads) and a third of an SM's shared memory
+        bp.p.L = (int)std::min<long long>(64, std::max(1LL, bp.p.nlines));
+        if (!fit_pass_threads(&bp.p, pl->arith, BATCH_THREADS, 72 * 1024)) {
           report("batch: a pass needs more threads than the batched launch has");
           free_batch(b);
           return nullptr;

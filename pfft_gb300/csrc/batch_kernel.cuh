@@ -13,7 +13,7 @@
 // can see a stale L1 line.
 //
 // A tile is either a register-resident radix-8 tile (power-of-two c2c lines
-// of 64..512 points, BATCH_THREADS = L * N/8 threads) or a general pass tile.
+// of 16..512 points, BATCH_THREADS = L * N/8 threads) or a general pass tile.
 // The batch_*.cu units are compiled as relocatable device code.
 #pragma once
 #include <type_traits>
@@ -55,8 +55,8 @@ __host__ __device__ constexpr int batch_fast_lines(int N) { return BATCH_THREADS
 
 // Radix-8 tiles are expanded inline (they are register-resident and short);
 // the general tiles are separate device functions in their own translation
-// units (batch_tiles_gen_*.cu, relocatable device code, at most 128 registers
-// so that two 256-thread blocks fit an SM): each is compiled once, in
+// units (batch_tiles_gen_*.cu, relocatable device code, at most 80 registers
+// so that three 256-thread blocks fit an SM): each is compiled once, in
 // parallel with the rest of the build.
 #define PG_BT_GEN(name) __device__ void name(const PassParams& p, long long tile, unsigned char* sm)
 PG_BT_GEN(bt_gen_f32_m);
@@ -88,6 +88,8 @@ template <bool DOUBLE>
 __device__ __forceinline__ void batch_fast(const BatchPass& bp, long long tile, unsigned char* sm) {
   typedef typename std::conditional<DOUBLE, fast::FDD, fast::F32>::type P;
   switch (bp.fastN) {
+    case 16: batch_fast_n<P, 16>(bp, tile, sm); break;
+    case 32: batch_fast_n<P, 32>(bp, tile, sm); break;
     case 64: batch_fast_n<P, 64>(bp, tile, sm); break;
     case 128: batch_fast_n<P, 128>(bp, tile, sm); break;
     case 256: batch_fast_n<P, 256>(bp, tile, sm); break;
@@ -99,7 +101,7 @@ __device__ __forceinline__ void batch_fast(const BatchPass& bp, long long tile, 
 // pass carries its own arithmetic (native FP64 for small plans, float-float
 // for large ones).
 template <bool DOUBLE>
-__global__ void __launch_bounds__(BATCH_THREADS, 2) k_batch(const BatchLaunch q) {
+__global__ void __launch_bounds__(BATCH_THREADS, 3) k_batch(const BatchLaunch q) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ int s_task;
   for (;;) {

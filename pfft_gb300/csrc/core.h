@@ -175,8 +175,9 @@ void apply_wisdom(PassProgram* prog, int arith);
 bool tune_program(Plan* pl, PassProgram* prog);
 // Re-plan the general kernel of a pass (radix order, lines per CTA).
 bool refit_pass(PassParams* p, int arith, int pref, int L);
-// Re-fit a general pass to at most max_threads threads (batched launches).
-bool fit_pass_threads(PassParams* p, int arith, int max_threads);
+// Re-fit a general pass to at most max_threads threads and max_smem bytes of
+// shared memory, halving its lines per CTA from p->L (batched launches).
+bool fit_pass_threads(PassParams* p, int arith, int max_threads, int max_smem);
 // Run a program with resolved buffers.  Returns a cudaError_t value.
 int run_program(Plan* pl, const PassProgram& prog, void* in, void* out, cudaStream_t s);
 // Ensure workspace capacity for a program.

@@ -8,7 +8,7 @@ bool fast_args(const PassParams& p, int arith, FastArgs* a, bool* row_in, bool* 
   if (p.mode != MODE_C2C || p.nst == 0) return false;
   if (p.M != p.N || p.Ni != p.N || p.No != p.N || p.Zi || p.Zo || p.wmode) return false;
   const int N = p.N;
-  if (N < 64 || N > 4096 || (N & (N - 1))) return false;
+  if (N < 16 || N > 4096 || (N & (N - 1))) return false;
   if (arith != ARITH_F32 && arith != ARITH_DF) return false;
   if (p.ashI.en || p.ashO.en) return false;
   if (p.nb > PG_MAX_BATCH) return false;

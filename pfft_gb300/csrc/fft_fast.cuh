@@ -1,4 +1,4 @@
-// Register-resident radix-8 pass for power-of-two c2c lines (64..4096).
+// Register-resident radix-8 pass for power-of-two c2c lines (16..4096).
 //
 // The generic pass (fft_pass.cu) stages every stage through shared memory and
 // handles every mode.  This kernel covers the hot case - a plain c2c line
@@ -164,8 +164,8 @@ __device__ __forceinline__ void bf8(typename P::C* v) {
 
 __device__ __forceinline__ int pad(int p) { return p + (p >> 3); }
 
-__host__ __device__ constexpr int n8_of(int N) { return N >= 4096 ? 4 : (N >= 512 ? 3 : 2); }
-__host__ __device__ constexpr int pow8(int a) { return a == 4 ? 4096 : (a == 3 ? 512 : 64); }
+__host__ __device__ constexpr int n8_of(int N) { return N >= 4096 ? 4 : (N >= 512 ? 3 : (N >= 64 ? 2 : 1)); }
+__host__ __device__ constexpr int pow8(int a) { return a == 4 ? 4096 : (a == 3 ? 512 : (a == 2 ? 64 : 8)); }
 
 struct FastArgs {
   const void* src;

@@ -8,6 +8,8 @@ template <class P, int SIGN>
 int launch_small(int N, const FastArgs& a, bool row_in, bool row_out, cudaStream_t s) {
   const bool col = !(row_in && row_out);
   switch (N) {
+    case 16: return launch4<P, SIGN, 16, 128>(a, row_in, row_out, s);
+    case 32: return launch4<P, SIGN, 32, 64>(a, row_in, row_out, s);
     case 64: return launch4<P, SIGN, 64, 32>(a, row_in, row_out, s);
     case 128: return launch4<P, SIGN, 128, 16>(a, row_in, row_out, s);
     case 256: return launch4<P, SIGN, 256, 8>(a, row_in, row_out, s);

@@ -8,23 +8,43 @@
 // with table twiddles, and any other prime uses a shared-memory ping-pong stage.
 #include <stdlib.h>
 #include <string.h>
+#include <atomic>
 #include "pass_tile.cuh"
 
 namespace pg {
+
+// The dynamic shared-memory limit is raised once per kernel, device and size
+// (an attribute call costs microseconds; small transforms launch often).
+template <const void* (*KFN)()>
+static int ensure_smem_attr(int bytes) {
+  static std::atomic<int> done[64];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (done[dev].load(std::memory_order_relaxed) >= bytes) return 0;
+  cudaError_t e = cudaFuncSetAttribute(KFN(), cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e != cudaSuccess) return (int)e;
+  int cur = done[dev].load();
+  while (cur < bytes && !done[dev].compare_exchange_weak(cur, bytes)) {
+  }
+  return 0;
+}
+template <class A, int SIGN>
+static const void* kptr() {
+  return (const void*)k_pass<A, SIGN>;
+}
 
 template <class A>
 static int launch_t(const PassParams& p, cudaStream_t stream) {
   long long grid = (p.nlines + p.L - 1) / p.L;
   if (grid <= 0) return 0;
   if (grid > 2147483647LL) return (int)cudaErrorInvalidConfiguration;
-  cudaError_t err;
+  int rc;
   if (p.sign < 0) {
-    err = cudaFuncSetAttribute(k_pass<A, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, p.smem_bytes);
-    if (err != cudaSuccess) return (int)err;
+    if ((rc = ensure_smem_attr<kptr<A, -1>>(p.smem_bytes))) return rc;
     k_pass<A, -1><<<(unsigned)grid, p.threads, p.smem_bytes, stream>>>(p);
   } else {
-    err = cudaFuncSetAttribute(k_pass<A, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, p.smem_bytes);
-    if (err != cudaSuccess) return (int)err;
+    if ((rc = ensure_smem_attr<kptr<A, 1>>(p.smem_bytes))) return rc;
     k_pass<A, 1><<<(unsigned)grid, p.threads, p.smem_bytes, stream>>>(p);
   }
   return (int)cudaGetLastError();

@@ -14,7 +14,13 @@
 
 namespace pg {
 
-#define PG_MAXE 16
+// Complex values a thread holds in registers in one register stage: 16 for
+// FP32, 8 for float-float and FP64 (whose values are twice as wide), so that
+// the stage fits the register file without spilling.
+template <class A>
+__host__ __device__ constexpr int max_elems() {
+  return A::kId == ARITH_F32 ? 16 : 8;
+}
 
 template <class A, bool CG = false>
 struct K {
@@ -173,7 +179,7 @@ struct K {
   // One register-staged Stockham stage of radix R_ over L lines.
   template <int SIGN, int R_>
   static __device__ __forceinline__ void reg_stage(S* buf, int L, int M, int LS, int Ns, const S* t) {
-    constexpr int NB = PG_MAXE / R_;
+    constexpr int NB = max_elems<A>() / R_ > 0 ? max_elems<A>() / R_ : 1;
     C v[NB][R_];
     int jj[NB], ll[NB];
     const int MR = M / R_;

@@ -105,11 +105,14 @@ bool factorize(int M, int* radix, int* nst, bool* generic, int pref) {
   return *nst < PG_MAX_STAGES;
 }
 
-int stage_threads(int R, long long work /* L*M */) {
+// Threads a register stage of radix R needs over `work` = L*M points: each
+// thread holds max_elems/R butterflies (at least one); max_elems is 16
+// complex values for FP32 and 8 for float-float / FP64 (pass_tile.cuh).
+int stage_threads(int R, long long work /* L*M */, int arith) {
+  const int maxe = arith == ARITH_F32 ? 16 : 8;
   int nb;
   switch (R) {
-    case 2: case 4: case 8: case 16: nb = 16 / R; break;
-    case 3: case 5: case 7: case 11: case 13: nb = 16 / R; break;
+    case 2: case 3: case 4: case 5: case 7: case 8: case 11: case 13: case 16: nb = std::max(1, maxe / R); break;
     default: return 0;  // generic stage: any thread count
   }
   long long bfly = work / R;
@@ -167,7 +170,7 @@ bool refit_pass(PassParams* p, int arith, int pref, int L) {
   q.pingpong = generic ? 1 : 0;
   if (L > 0) q.L = (int)std::min<long long>(L, std::max(1LL, q.nlines));
   int T = 64;
-  for (int st = 0; st < q.nst; st++) T = std::max(T, stage_threads(q.radix[st], (long long)q.L * q.M));
+  for (int st = 0; st < q.nst; st++) T = std::max(T, stage_threads(q.radix[st], (long long)q.L * q.M, arith));
   T = (T + 31) / 32 * 32;
   if (T > 512) return false;
   long long meta = ((2 * 8 + 2 * 4) * (long long)q.L + 15) & ~15LL;
@@ -182,17 +185,18 @@ bool refit_pass(PassParams* p, int arith, int pref, int L) {
 // Re-fit a general pass to at most max_threads threads per CTA (the
 // batched persistent launch runs every tile with one block size): halve the
 // lines per tile until every register stage's butterflies are covered.
-bool fit_pass_threads(PassParams* p, int arith, int max_threads) {
+bool fit_pass_threads(PassParams* p, int arith, int max_threads, int max_smem) {
   long long L = p->L;
   for (;;) {
     int T = 32;
-    for (int st = 0; st < p->nst; st++) T = std::max(T, stage_threads(p->radix[st], L * p->M));
+    for (int st = 0; st < p->nst; st++) T = std::max(T, stage_threads(p->radix[st], L * p->M, arith));
     T = (T + 31) / 32 * 32;
-    if (T <= max_threads) {
+    long long meta = ((2 * 8 + 2 * 4) * L + 15) & ~15LL;
+    long long smem = meta + L * p->LS * (long long)arith_sm_bytes(arith) * (p->pingpong ? 2 : 1);
+    if (T <= max_threads && (smem <= max_smem || L == 1)) {
       p->L = (int)L;
       p->threads = T;
-      long long meta = ((2 * 8 + 2 * 4) * L + 15) & ~15LL;
-      p->smem_bytes = (int)(meta + L * p->LS * (long long)arith_sm_bytes(arith) * (p->pingpong ? 2 : 1));
+      p->smem_bytes = (int)smem;
       return true;
     }
     if (L == 1) return false;
@@ -480,7 +484,7 @@ bool build_program(const PlanDesc& d, int arith, bool inplace, bool adjoint, Pas
     bool generic = false;
     if (s.identity) {
       p.nst = 0;
-    } else if (!factorize(s.M, p.radix, &p.nst, &generic, 0)) {
+    } else if (!factorize(s.M, p.radix, &p.nst, &generic, arith == ARITH_F32 ? 0 : 1)) {
       set_error(7, "transform length has too many factors");
       return false;
     }
@@ -490,11 +494,14 @@ bool build_program(const PlanDesc& d, int arith, bool inplace, bool adjoint, Pas
     long long L = std::max(1LL, 65536 / line_bytes);
     if (!(p.in_contig && p.out_contig)) L = std::max(L, std::min(8LL, 163840 / line_bytes));
     L = std::min(L, 64LL);
+    // small problems: keep at least two CTAs per SM (152 SMs) so that a pass
+    // is not one latency-bound wave of a few CTAs
+    L = std::min(L, std::max(1LL, (p.nlines + 303) / 304));
     L = std::max(1LL, std::min(L, p.nlines));
     int T = 0;
     for (;;) {
       T = 64;
-      for (int st = 0; st < p.nst; st++) T = std::max(T, stage_threads(p.radix[st], L * s.M));
+      for (int st = 0; st < p.nst; st++) T = std::max(T, stage_threads(p.radix[st], L * s.M, arith));
       T = (T + 31) / 32 * 32;
       if (T <= 512 || L == 1) break;
       L = std::max(1LL, L / 2);

@@ -3,7 +3,10 @@
 C1  64^3 c2c complex128, forward then backward / N^3, against the oracle.
 C2  256^3 r2c / c2r, float64 and float32, N(0,1) real input, PADDED_R2C
     in place, forward TRANSPOSED_OUT, backward TRANSPOSED_IN, against the
-    oracle; plus REDFT10 (and its inverse REDFT01) on the same shape.
+    oracle; plus REDFT10 (and its inverse REDFT01) on the same shape, against
+    scipy.fft.dctn (pocketfft, an independent implementation of the same
+    definitions: the oracle evaluates r2r lines directly, O(n^2) per line, and
+    is checked against scipy at smaller sizes).
 C5  512^3 complex128 and 1024^3 complex64 forward + backward (size-independent
     properties: round trip and Parseval), 64^4 complex128 against the oracle.
 
@@ -58,8 +61,9 @@ def test_c2_256cube_redft10(cuda, pfft_lib, prec, tol):
     x = rng.standard_normal(256 ** 3)
     if prec == "float":
         x = x.astype(np.float32).astype(np.float64)
+    sfft = pytest.importorskip("scipy.fft")
     y = gpu_run(fwd, x, prec=prec)
-    ref = oracle_run(fwd, x)
+    ref = sfft.dctn(x.reshape(n), type=2, workers=-1).ravel()  # = FFTW REDFT10
     assert rel_l2(y, ref) <= tol
     back = Req("r2r", n, kinds=[4, 4, 4])  # REDFT01, inverse up to (2n)^3
     z = gpu_run(back, ref, prec=prec) / (2 * 256) ** 3

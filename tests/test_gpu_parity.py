@@ -161,7 +161,8 @@ def test_double_arith_modes(cuda, pfft_lib):
     assert L.pfft_gb300_get_double_arith() == old
 
 
-@pytest.mark.parametrize("n,flags", [((64, 64, 64), 0), ((128, 64, 256), TO), ((512, 8, 16), 0),
+@pytest.mark.parametrize("n,flags", [((32, 32, 32), 0), ((16, 32, 64), TO), ((64, 64, 64), 0), ((128, 64, 256), TO),
+                                     ((512, 8, 16), 0),
                                      ((16, 1024, 8), TI), ((2048, 4, 4), 0), ((8, 4, 4096), 0)])
 @pytest.mark.parametrize("prec", PRECS)
 def test_kernel_paths_agree(cuda, pfft_lib, n, flags, prec):

@@ -227,3 +227,16 @@ def test_layout_reference_values():
     # 3-D data on a 3-D mesh: real rows are reported unpadded
     mem, lni, _, lno, _ = LO.local_size(3, [8, 8, 8], [8, 8, 8], [8, 8, 8], 1, LO.R2C, 1 << 11, 3)
     assert lni == [8, 8, 8] and lno == [8, 8, 5] and mem == 512
+
+
+def test_r2r_3d_vs_scipy():
+    """The oracle's multi-axis r2r (REDFT10 / REDFT01 / RODFT00 on 32x24x20)
+    against scipy.fft's n-dimensional DCT/DST."""
+    import scipy.fft as sf
+    from tests.pfft_util import Req, oracle_run, rel_l2
+    n = (32, 24, 20)
+    x = np.random.default_rng(7).standard_normal(int(np.prod(n)))
+    for kinds, fn in (([5, 5, 5], lambda a: sf.dctn(a, type=2)), ([4, 4, 4], lambda a: sf.dctn(a, type=3)),
+                      ([7, 7, 7], lambda a: sf.dstn(a, type=1))):
+        y = oracle_run(Req("r2r", n, kinds=kinds), x)
+        assert rel_l2(y, fn(x.reshape(n)).ravel()) < 1e-14
