@@ -2,7 +2,8 @@
 
 Workload (one step): one forward pfft_execute of a 512^3 complex128 c2c
 transform on a 1x1 process mesh, out of place, standard layout - the
-configuration the headline target is quoted on.  Inputs are uniform[-1,1)
+configuration the headline target is quoted on.  The plan is made with
+PFFT_PATIENT (the autotuner runs at planning time, outside the timed region).  Inputs are uniform[-1,1)
 from a fixed seed, 2.1 GB per array (larger than the 129 MB L2, so no flush is
 needed between steps).
 
@@ -328,6 +329,9 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--n", type=int, default=512, help="cube edge (profiling runs use a smaller case)")
     ap.add_argument("--shape", default=None, help="n0xn1xn2 instead of a cube (profiling runs)")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="plan with PFFT_MEASURE instead of PFFT_PATIENT (by default the autotuner times every "
+                         "pass's candidates at planning time, before the timed region)")
     ap.add_argument("--prec", default="double", choices=["double", "float"],
                     help="double = pfft_ (complex128, the headline); float = pfftf_ (complex64)")
     args = ap.parse_args()
@@ -353,8 +357,8 @@ def main():
     a = host.to(dev)
     b = torch.empty_like(a)
     comm = pg.procmesh(2)
-    plan = getattr(L, pre + "plan_dft_3d")(pg.ints(n), a.data_ptr(), b.data_ptr(), comm, pg.PFFT_FORWARD,
-                                           pg.PFFT_TRANSPOSED_NONE | pg.PFFT_MEASURE)
+    plan_flags = pg.PFFT_TRANSPOSED_NONE | (pg.PFFT_MEASURE if args.no_tune else pg.PFFT_PATIENT)
+    plan = getattr(L, pre + "plan_dft_3d")(pg.ints(n), a.data_ptr(), b.data_ptr(), comm, pg.PFFT_FORWARD, plan_flags)
     if not plan:
         raise RuntimeError("plan failed: %s" % (pg.last_error(),))
     stream = torch.cuda.Stream(device=dev)
@@ -448,7 +452,7 @@ def main():
         "config": {"workload": "pfft_execute c2c %s %s forward, 1x1 procmesh, out-of-place, "
                                "TRANSPOSED_NONE" % ("x".join(map(str, n)) if args.shape else "%d^3" % args.n,
                                                     "complex128" if args.prec == "double" else "complex64"),
-                   "bytes_per_step": B, "p_min": pmin,
+                   "bytes_per_step": B, "p_min": pmin, "planner": "PFFT_MEASURE" if args.no_tune else "PFFT_PATIENT (autotuned at planning time)",
                    "l2": "arrays (%.2f GB each) larger than the 129 MB L2; no flush" % (cnt * esz / 1e9),
                    "parallelism": "replicas" if world > 1
                    else "single GPU"},

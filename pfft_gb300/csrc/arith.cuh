@@ -104,43 +104,37 @@ __device__ __forceinline__ df df_from_double(double x) {
   return {hi, lo};
 }
 
-// float -> double bit pattern, exact, integer operations only (normal floats
-// and zero; subnormal floats are flushed to zero).
-__device__ __forceinline__ unsigned long long f2d_bits(float f) {
-  unsigned u = __float_as_uint(f);
-  unsigned long long s = (unsigned long long)(u >> 31) << 63;
-  unsigned ef = (u >> 23) & 0xFF;
-  if (ef == 0) return s;
-  if (ef == 255) return s | 0x7FF0000000000000ull | ((unsigned long long)(u & 0x7FFFFF) << 29);
-  return s | ((unsigned long long)(ef + 896) << 52) | ((unsigned long long)(u & 0x7FFFFF) << 29);
-}
-
-// float-float -> double with integer operations only.  The pair is first
-// renormalised (|lo| <= ulp(hi)/2), so lo adds fewer than 2^29 units of the
-// double's last place to hi's 53-bit mantissa; low bits are truncated.
+// float-float -> double without FP64 instructions.  After renormalising
+// (|lo| <= ulp(hi)/2), lo is turned into a signed integer count L of the last
+// place of hi's double (|L| <= 2^28) by an exact power-of-two scaling and one
+// float -> int conversion (round to nearest), and L is added to the bit
+// pattern of hi as a double: the sum, correctly rounded.  The sum never leaves
+// hi's binade upwards; downwards only when hi is a power of two and lo has
+// the opposite sign, where the lower binade's last place is half as large and
+// the scale doubles.  Below 2^-74 the scale 2^(52-e) would overflow a float
+// and is applied in two steps.  Results below 2^-126 are flushed to zero.
 __device__ __forceinline__ double df_to_double(df v) {
   const float hi = __fadd_rn(v.hi, v.lo);
   const float lo = __fsub_rn(v.lo, __fsub_rn(hi, v.hi));
-  const unsigned uh = __float_as_uint(hi);
-  const unsigned eh = (uh >> 23) & 0xFF;
-  if (eh == 0 || eh == 255) return __longlong_as_double((long long)f2d_bits(hi));
-  const unsigned ul = __float_as_uint(lo);
-  const unsigned el = (ul >> 23) & 0xFF;
-  unsigned L = 0;
-  if (el != 0) {
-    const unsigned ml = (ul & 0x7FFFFFu) | 0x800000u;
-    const int sh = (int)el - (int)eh + 29;  // <= 5
-    L = sh >= 0 ? (ml << sh) : (sh > -24 ? (ml >> (-sh)) : 0u);
+  const unsigned uh = __float_as_uint(hi), ul = __float_as_uint(lo);
+  const unsigned ehb = uh & 0x7F800000u;
+  const bool opp = ((uh ^ ul) & 0x80000000u) != 0u;
+  unsigned sb = (306u << 23) - ehb;                    // 2^(52 - e_hi)
+  if (opp && (uh & 0x7FFFFFu) == 0u) sb += 1u << 23;   // lower binade: twice the scale
+  float lf;
+  if ((sb >> 23) <= 254u) {
+    lf = __fmul_rn(lo, __uint_as_float(sb));
+  } else {
+    lf = __fmul_rn(__fmul_rn(lo, __uint_as_float((127u + 64u) << 23)), __uint_as_float(sb - (64u << 23)));
   }
-  unsigned long long M = (unsigned long long)((uh & 0x7FFFFFu) | 0x800000u) << 29;
-  M = (((uh ^ ul) >> 31) == 0) ? M + L : M - L;
-  unsigned long long E = eh + 896;
-  if (M < (1ull << 52)) {  // a borrow moved the leading one down
-    M <<= 1;
-    E -= 1;
-  }
-  return __longlong_as_double((long long)(((unsigned long long)(uh >> 31) << 63) | (E << 52) |
-                                          (M & 0xFFFFFFFFFFFFFull)));
+  int L = __float2int_rn(lf);
+  if (uh & 0x80000000u) L = -L;  // count in the direction of hi's magnitude
+  const unsigned dh = (uh & 0x80000000u) | (((uh & 0x7FFFFFFFu) >> 3) + (896u << 20));
+  unsigned long long P = (((unsigned long long)dh << 32) | (uh << 29)) + (unsigned long long)(long long)L;
+  if (ehb == 0u) P = (unsigned long long)(uh & 0x80000000u) << 32;
+  if (ehb == 0x7F800000u)
+    P = ((unsigned long long)((uh & 0x80000000u) | 0x7FF00000u | ((uh & 0x7FFFFFu) >> 3)) << 32) | (uh << 29);
+  return __longlong_as_double((long long)P);
 }
 
 // ---------------------------------------------------------------------------

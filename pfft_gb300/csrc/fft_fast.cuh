@@ -179,7 +179,8 @@ struct FastArgs {
   long long nlines;
   int conj_in, conj_out;
   int in_df, out_df;  // double API: the array holds float-float pairs (an intermediate)
-  int fastL;          // requested lines per CTA (0: default); 512 takes 4 or 8, 1024 takes 2 or 4
+  int fastL;          // requested lines per CTA (0: default): 512 takes 4, 8, 16; 1024 takes 2, 4, 8;
+                      // 2048 takes 2, 4; 4096 takes 1, 2
 };
 
 // global element access: native format, or float-float pairs for the

@@ -15,6 +15,7 @@ int launch_small(int N, const FastArgs& a, bool row_in, bool row_out, cudaStream
     case 256: return launch4<P, SIGN, 256, 8>(a, row_in, row_out, s);
     case 512: {
       const int L = a.fastL ? a.fastL : (col ? 8 : 4);
+      if (L == 16) return launch4<P, SIGN, 512, 16>(a, row_in, row_out, s);
       return L == 8 ? launch4<P, SIGN, 512, 8>(a, row_in, row_out, s) : launch4<P, SIGN, 512, 4>(a, row_in, row_out, s);
     }
   }

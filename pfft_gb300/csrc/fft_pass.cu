@@ -33,19 +33,34 @@ template <class A, int SIGN>
 static const void* kptr() {
   return (const void*)k_pass<A, SIGN>;
 }
+template <class A, int SIGN>
+static const void* kptr_small() {
+  return (const void*)k_pass_small<A, SIGN>;
+}
 
 template <class A>
 static int launch_t(const PassParams& p, cudaStream_t stream) {
   long long grid = (p.nlines + p.L - 1) / p.L;
   if (grid <= 0) return 0;
   if (grid > 2147483647LL) return (int)cudaErrorInvalidConfiguration;
+  const bool small = pass_is_small(p);
   int rc;
   if (p.sign < 0) {
-    if ((rc = ensure_smem_attr<kptr<A, -1>>(p.smem_bytes))) return rc;
-    k_pass<A, -1><<<(unsigned)grid, p.threads, p.smem_bytes, stream>>>(p);
+    if (small) {
+      if ((rc = ensure_smem_attr<kptr_small<A, -1>>(p.smem_bytes))) return rc;
+      k_pass_small<A, -1><<<(unsigned)grid, p.threads, p.smem_bytes, stream>>>(p);
+    } else {
+      if ((rc = ensure_smem_attr<kptr<A, -1>>(p.smem_bytes))) return rc;
+      k_pass<A, -1><<<(unsigned)grid, p.threads, p.smem_bytes, stream>>>(p);
+    }
   } else {
-    if ((rc = ensure_smem_attr<kptr<A, 1>>(p.smem_bytes))) return rc;
-    k_pass<A, 1><<<(unsigned)grid, p.threads, p.smem_bytes, stream>>>(p);
+    if (small) {
+      if ((rc = ensure_smem_attr<kptr_small<A, 1>>(p.smem_bytes))) return rc;
+      k_pass_small<A, 1><<<(unsigned)grid, p.threads, p.smem_bytes, stream>>>(p);
+    } else {
+      if ((rc = ensure_smem_attr<kptr<A, 1>>(p.smem_bytes))) return rc;
+      k_pass<A, 1><<<(unsigned)grid, p.threads, p.smem_bytes, stream>>>(p);
+    }
   }
   return (int)cudaGetLastError();
 }

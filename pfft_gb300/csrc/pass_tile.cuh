@@ -287,7 +287,9 @@ struct K {
   }
 
   // value of the length-M sequence at position pos for line l
+  template <bool C2C_ONLY = false>
   static __device__ __forceinline__ C gather(const PassParams& p, long long off, int pos, int lsg) {
+    if (C2C_ONLY) return xc(p, off, pos, lsg);
     const int N = p.N, M = p.M;
     switch (p.mode) {
       case MODE_C2C:
@@ -350,10 +352,11 @@ struct K {
   }
 
   // output element k (logical index o = Zo + k) of line l
+  template <bool C2C_ONLY = false>
   static __device__ __forceinline__ void scatter(const PassParams& p, const S* line, long long off, int k, int lsg) {
     const int o = p.Zo + k;
     const int sg = lsg * shsign(p.ashO, k);
-    switch (p.mode) {
+    switch (C2C_ONLY ? (int)MODE_C2C : p.mode) {
       case MODE_C2C:
       case MODE_R2C: {
         C v = A::lds(line[o]);
@@ -412,7 +415,10 @@ struct K {
 // One tile (L lines) of a pass.  smraw: dynamic shared memory of at least
 // p.smem_bytes.  CG: read global memory through L2 only (batched launches,
 // where the input was written by other CTAs of the same launch).
-template <class A, int SIGN, bool CG>
+// SMALL: a c2c pass with radices 2, 3, 4, 5, 7 and 8 only (no 11, 13, 16 or
+// generic-prime stage, no real-data modes); the kernel then needs far fewer
+// registers.
+template <class A, int SIGN, bool CG, bool SMALL = false>
 __device__ __forceinline__ void pass_tile(const PassParams& p, long long tile, unsigned char* smraw) {
   typedef K<A, CG> KK;
   typedef typename A::sm_t S;
@@ -456,13 +462,13 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, long long tile, u
     for (int e = threadIdx.x; e < tot; e += blockDim.x) {
       int l = e / M;
       int pos = e - l * M;
-      buf[l * p.LS + pos] = A::sts(KK::gather(p, offI[l], pos, sgI[l]));
+      buf[l * p.LS + pos] = A::sts(KK::template gather<SMALL>(p, offI[l], pos, sgI[l]));
     }
   } else {
     for (int e = threadIdx.x; e < tot; e += blockDim.x) {
       int pos = e / L;
       int l = e - pos * L;
-      buf[l * p.LS + pos] = A::sts(KK::gather(p, offI[l], pos, sgI[l]));
+      buf[l * p.LS + pos] = A::sts(KK::template gather<SMALL>(p, offI[l], pos, sgI[l]));
     }
   }
   __syncthreads();
@@ -481,10 +487,10 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, long long tile, u
       case 5: KK::template reg_stage<SIGN, 5>(cur, L, M, p.LS, Ns, t); break;
       case 7: KK::template reg_stage<SIGN, 7>(cur, L, M, p.LS, Ns, t); break;
       case 8: KK::template reg_stage<SIGN, 8>(cur, L, M, p.LS, Ns, t); break;
-      case 11: KK::template reg_stage<SIGN, 11>(cur, L, M, p.LS, Ns, t); break;
-      case 13: KK::template reg_stage<SIGN, 13>(cur, L, M, p.LS, Ns, t); break;
-      case 16: KK::template reg_stage<SIGN, 16>(cur, L, M, p.LS, Ns, t); break;
-      default: {
+      case 11: if (!SMALL) KK::template reg_stage<SIGN, 11>(cur, L, M, p.LS, Ns, t); break;
+      case 13: if (!SMALL) KK::template reg_stage<SIGN, 13>(cur, L, M, p.LS, Ns, t); break;
+      case 16: if (!SMALL) KK::template reg_stage<SIGN, 16>(cur, L, M, p.LS, Ns, t); break;
+      default: if (!SMALL) {
         KK::template generic_stage<SIGN>(cur, alt, L, M, p.LS, Ns, R_, t);
         S* tmp = cur;
         cur = alt;
@@ -501,13 +507,13 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, long long tile, u
     for (int e = threadIdx.x; e < toto; e += blockDim.x) {
       int l = e / No;
       int k = e - l * No;
-      KK::scatter(p, cur + l * p.LS, offO[l], k, sgO[l]);
+      KK::template scatter<SMALL>(p, cur + l * p.LS, offO[l], k, sgO[l]);
     }
   } else {
     for (int e = threadIdx.x; e < toto; e += blockDim.x) {
       int k = e / L;
       int l = e - k * L;
-      KK::scatter(p, cur + l * p.LS, offO[l], k, sgO[l]);
+      KK::template scatter<SMALL>(p, cur + l * p.LS, offO[l], k, sgO[l]);
     }
   }
 }
@@ -517,6 +523,24 @@ template <class A, int SIGN>
 __global__ void __launch_bounds__(512) k_pass(const PassParams p) {
   extern __shared__ __align__(16) unsigned char smraw[];
   pass_tile<A, SIGN, false>(p, blockIdx.x, smraw);
+}
+
+// The same for passes of radices 2..8 only, at two CTAs of up to 512
+// threads per SM (at most 64 registers).
+template <class A, int SIGN>
+__global__ void __launch_bounds__(512, 2) k_pass_small(const PassParams p) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  pass_tile<A, SIGN, false, true>(p, blockIdx.x, smraw);
+}
+
+// true for a c2c pass whose every stage has radix 2, 3, 4, 5, 7 or 8
+inline bool pass_is_small(const PassParams& p) {
+  if (p.pingpong || p.mode != MODE_C2C) return false;
+  for (int s = 0; s < p.nst; s++) {
+    const int r = p.radix[s];
+    if (r != 2 && r != 3 && r != 4 && r != 5 && r != 7 && r != 8) return false;
+  }
+  return true;
 }
 
 }  // namespace pg

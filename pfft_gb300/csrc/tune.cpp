@@ -1,7 +1,8 @@
 // Autotuner and wisdom.
 //
 // A pass can run with several equivalent configurations: the register-resident
-// radix-8 kernel (with 4 or 8 lines per CTA at 512 points, 2 or 4 at 1024) or
+// radix-8 kernel (4, 8 or 16 lines per CTA at 512 points, 2, 4 or 8 at 1024,
+// 2 or 4 at 2048, 1 or 2 at 4096) or
 // the general kernel with radix order 16-first / 8-first / 4-first and half,
 // the planned or twice the planned lines per CTA.  Plans created with
 // PFFT_PATIENT, PFFT_EXHAUSTIVE or PFFT_TUNE time every candidate of every
@@ -73,9 +74,14 @@ std::vector<Choice> candidates(const PassParams& p, int arith) {
   if (fast_pass_eligible(q, arith)) {
     Choice c;
     v.push_back(c);
-    if (p.N == 512 || p.N == 1024) {
-      const bool col = !(p.sIa == 1 && p.sOa == 1);
-      c.fastL = p.N == 512 ? (col ? 4 : 8) : (col ? 2 : 4);  // the non-default tile height
+    // the other tile heights instantiated for this length (fft_fast_*_[sl].cu)
+    std::vector<int> alt;
+    if (p.N == 512) alt = {4, 8, 16};
+    if (p.N == 1024) alt = {2, 4, 8};
+    if (p.N == 2048) alt = {2, 4};
+    if (p.N == 4096) alt = {1, 2};
+    for (int Lf : alt) {
+      c.fastL = Lf;
       v.push_back(c);
     }
   }
