@@ -107,7 +107,8 @@ Batch* make_batch(Plan* const* plans, int n) {
         bp.frow = ri ? 1 : 0;
         const int L = batch_fast_lines(bp.fastN);
         tiles = (ps.p.nlines + L - 1) / L;
-        b->smem = std::max(b->smem, (int)(16 * L + (size_t)L * (bp.fastN + bp.fastN / 8 + 1) * fsz));
+        const int lsp = fsz == 8 ? bp.fastN + 16 : bp.fastN + bp.fastN / 8 + 4;  // as fast_smem_bytes
+        b->smem = std::max(b->smem, (int)(16 * L + (size_t)L * lsp * fsz));
         b->fast_passes++;
       } else {
         bp.fastN = 0;
@@ -121,6 +122,7 @@ Batch* make_batch(Plan* const* plans, int n) {
           return nullptr;
         }
         tiles = (bp.p.nlines + bp.p.L - 1) / bp.p.L;
+        bp.small = pass_is_small(bp.p) ? 1 : 0;
         b->smem = std::max(b->smem, bp.p.smem_bytes);
       }
       b->bytes += ps.bytes;

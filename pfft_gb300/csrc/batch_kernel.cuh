@@ -38,6 +38,7 @@ struct BatchPass {
   int frow;          // radix-8 tile: 1 = lines contiguous on both sides, 0 = columns
   int done;          // counter this pass increments
   int arith;         // arithmetic of the pass's plan
+  int small;         // general tile of a c2c pass with radices <= 8 (pass_is_small)
 };
 
 struct BatchLaunch {
@@ -65,8 +66,16 @@ PG_BT_GEN(bt_gen_df_m);
 PG_BT_GEN(bt_gen_df_p);
 PG_BT_GEN(bt_gen_f64_m);
 PG_BT_GEN(bt_gen_f64_p);
+PG_BT_GEN(bt_small_f32_m);
+PG_BT_GEN(bt_small_f32_p);
+PG_BT_GEN(bt_small_df_m);
+PG_BT_GEN(bt_small_df_p);
+PG_BT_GEN(bt_small_f64_m);
+PG_BT_GEN(bt_small_f64_p);
 #define PG_BT_DEF_GEN(name, A, SIGN) \
   PG_BT_GEN(name) { pass_tile<A, SIGN, true>(p, tile, sm); }
+#define PG_BT_DEF_SMALL(name, A, SIGN) \
+  PG_BT_GEN(name) { pass_tile<A, SIGN, true, true>(p, tile, sm); }
 
 template <class P, int N>
 __device__ __forceinline__ void batch_fast_n(const BatchPass& bp, long long tile, unsigned char* sm) {
@@ -133,20 +142,20 @@ __global__ void __launch_bounds__(BATCH_THREADS, 3) k_batch(const BatchLaunch q)
     if (bp.fastN > 0) {
       batch_fast<DOUBLE>(bp, tile, sm);
     } else if (!DOUBLE) {
-      if (neg)
-        bt_gen_f32_m(bp.p, tile, sm);
+      if (bp.small)
+        neg ? bt_small_f32_m(bp.p, tile, sm) : bt_small_f32_p(bp.p, tile, sm);
       else
-        bt_gen_f32_p(bp.p, tile, sm);
+        neg ? bt_gen_f32_m(bp.p, tile, sm) : bt_gen_f32_p(bp.p, tile, sm);
     } else if (bp.arith == ARITH_F64) {
-      if (neg)
-        bt_gen_f64_m(bp.p, tile, sm);
+      if (bp.small)
+        neg ? bt_small_f64_m(bp.p, tile, sm) : bt_small_f64_p(bp.p, tile, sm);
       else
-        bt_gen_f64_p(bp.p, tile, sm);
+        neg ? bt_gen_f64_m(bp.p, tile, sm) : bt_gen_f64_p(bp.p, tile, sm);
     } else {
-      if (neg)
-        bt_gen_df_m(bp.p, tile, sm);
+      if (bp.small)
+        neg ? bt_small_df_m(bp.p, tile, sm) : bt_small_df_p(bp.p, tile, sm);
       else
-        bt_gen_df_p(bp.p, tile, sm);
+        neg ? bt_gen_df_m(bp.p, tile, sm) : bt_gen_df_p(bp.p, tile, sm);
     }
     __threadfence();
     __syncthreads();

@@ -8,10 +8,10 @@
 //   * stage 1 loading straight from global memory and the last stage storing
 //     straight to global memory, both coalesced (consecutive threads walk the
 //     contiguous direction: along the line for rows, across lines for
-//     columns); only the stages in between exchange through shared memory,
-//     double-buffered so each stage needs one barrier;
-//   * a padded shared-memory index p + p/8 that keeps the stride-8 Stockham
-//     writes free of bank conflicts;
+//     columns); only the stages in between exchange through shared memory
+//     (one buffer, two barriers per exchange);
+//   * a shared-memory layout (pad, lsp_of) that keeps the stage exchanges
+//     free of bank conflicts;
 //   * for the double API, float-float arithmetic with unnormalised additions
 //     (TwoSum on the high parts, plain sums of the low parts) renormalised
 //     once per butterfly output.
@@ -162,7 +162,29 @@ __device__ __forceinline__ void bf8(typename P::C* v) {
   v[7] = P::sub(e3, o3);
 }
 
-__device__ __forceinline__ int pad(int p) { return p + (p >> 3); }
+// Shared-memory layout of a tile: L lines at stride lsp_of, element p of a
+// line at index pad(p).  The layouts below make every stage exchange of the
+// kernel free of bank conflicts; they were chosen by simulating the
+// exchanges' shared-memory addresses (wavefronts per warp access) for every
+// instantiated length, tile height and orientation.
+//   FP32 (8-byte elements): an XOR swizzle of the low four bits by bits 3..6
+//     (a permutation of [0, N)); column tiles (adjacent lines in one warp)
+//     spread the lines' starts with 16/L extra elements, short row tiles hold
+//     several lines per warp and need N/8.
+//   float-float (16-byte elements): p + p/8 (one instruction: these kernels
+//     are bound by instruction issue) and a stride of N + N/8 + 1, with 2 or 4
+//     more for column tiles of 4 or 2 lines.
+template <class P>
+__device__ __forceinline__ int pad(int p) {
+  return sizeof(typename P::S) == 8 ? (p ^ ((p >> 3) & 15)) : (p + (p >> 3));
+}
+
+template <class P, int N, int L, bool ROW>
+__host__ __device__ constexpr int lsp_of() {
+  return sizeof(typename P::S) == 8
+             ? N + (ROW ? (N >= 128 ? 0 : (N == 64 ? 8 : N / 8)) : (L == 1 ? 0 : (16 / L > 1 ? 16 / L : 1)))
+             : N + N / 8 + (ROW ? (N <= 32 ? 0 : 1) : (L >= 8 || L == 1 ? 1 : (L == 4 ? 2 : 4)));
+}
 
 __host__ __device__ constexpr int n8_of(int N) { return N >= 4096 ? 4 : (N >= 512 ? 3 : (N >= 64 ? 2 : 1)); }
 __host__ __device__ constexpr int pow8(int a) { return a == 4 ? 4096 : (a == 3 ? 512 : (a == 2 ? 64 : 8)); }
@@ -229,8 +251,8 @@ __device__ __forceinline__ void gstore<FDD>(FDD::G* p, FDD::C v, int df) {
 // otherwise consecutive threads take consecutive (adjacent) lines.  ROW_OUT
 // likewise for the output; when they differ the last stage is re-staged
 // through shared memory so that both sides stay coalesced.
-// Shared memory: one buffer of L lines, line stride N + N/8 + 1 (odd, so the
-// lines of a warp fall on different banks), index p + p/8 within a line.
+// Shared memory: one buffer of L lines at stride lsp_of, index pad(p) within
+// a line.
 // One tile (L lines) of the pass, run by the L * N/8 threads of a block:
 // the body of the stand-alone kernel k_fast, and a task of the batched
 // persistent kernel.  `blk` is the tile index, `sm_raw` the block's dynamic
@@ -243,7 +265,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsi
   constexpr int TPL = N / 8;  // threads per line
   constexpr int NS8 = n8_of(N);
   constexpr int Q = N / pow8(NS8);  // last radix: 1, 2 or 4
-  constexpr int LSP = N + N / 8 + 1;
+  constexpr int LSP = lsp_of<P, N, L, ROW_IN>();
   long long* offI = (long long*)sm_raw;
   long long* offO = offI + L;
   S* buf = (S*)(sm_raw + 16 * L);
@@ -291,12 +313,12 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsi
       const int k = t % Ns;
       const int base = (t - k) * 8 + k;
 #pragma unroll
-      for (int r = 0; r < 8; r++) line[pad(base + r * Ns)] = P::sts(P::renorm(v[r]));
+      for (int r = 0; r < 8; r++) line[pad<P>(base + r * Ns)] = P::sts(P::renorm(v[r]));
     }
     __syncthreads();
     Ns *= 8;
 #pragma unroll
-    for (int r = 0; r < 8; r++) v[r] = P::lds(line[pad(t + r * TPL)]);
+    for (int r = 0; r < 8; r++) v[r] = P::lds(line[pad<P>(t + r * TPL)]);
     const int k = t % Ns;
     const int step = N / (Ns * 8);
 #pragma unroll
@@ -316,7 +338,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsi
     }
     __syncthreads();
 #pragma unroll
-    for (int r = 0; r < 8; r++) line[pad(t + r * TPL)] = P::sts(P::renorm(v[r]));
+    for (int r = 0; r < 8; r++) line[pad<P>(t + r * TPL)] = P::sts(P::renorm(v[r]));
   } else {
     // radix-Q stage (Q = 2 or 4) with Ns = N/Q: butterflies j = t + b*TPL, k = j
     if (NS8 > 1) __syncthreads();
@@ -324,7 +346,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsi
       const int k = t % Ns;
       const int base = (t - k) * 8 + k;
 #pragma unroll
-      for (int r = 0; r < 8; r++) line[pad(base + r * Ns)] = P::sts(P::renorm(v[r]));
+      for (int r = 0; r < 8; r++) line[pad<P>(base + r * Ns)] = P::sts(P::renorm(v[r]));
     }
     __syncthreads();
     constexpr int NB = 8 / Q;
@@ -335,7 +357,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsi
       const int j = t + b * TPL;
 #pragma unroll
       for (int r = 0; r < Q; r++) {
-        C x = P::lds(line[pad(j + r * NQ)]);
+        C x = P::lds(line[pad<P>(j + r * NQ)]);
         if (r > 0) x = P::mul(x, P::twc(__ldg(&tw[j * r]), SIGN));
         w[b * Q + r] = x;
       }
@@ -364,7 +386,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsi
 #pragma unroll
     for (int b = 0; b < NB; b++)
 #pragma unroll
-      for (int r = 0; r < Q; r++) line[pad(t + b * TPL + r * NQ)] = P::sts(P::renorm(w[b * Q + r]));
+      for (int r = 0; r < Q; r++) line[pad<P>(t + b * TPL + r * NQ)] = P::sts(P::renorm(w[b * Q + r]));
   }
   // re-staged store with the output's thread mapping
   __syncthreads();
@@ -377,7 +399,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsi
 #pragma unroll
       for (int r = 0; r < 8; r++) {
         const int k = t2 + r * TPL;
-        C o = P::lds(line2[pad(k)]);
+        C o = P::lds(line2[pad<P>(k)]);
         if (a.conj_out) o = P::conj(o);
         gstore<P>(d2 + (long long)k * a.sOa, o, a.out_df);
       }
@@ -393,7 +415,7 @@ __global__ void __launch_bounds__(L*(N / 8)) k_fast(const FastArgs a) {
 
 template <class P, int N, int L>
 constexpr size_t fast_smem_bytes() {
-  return 16 * L + (size_t)L * (N + N / 8 + 1) * sizeof(typename P::S);
+  return 16 * L + (size_t)L * (sizeof(typename P::S) == 8 ? N + 16 : N + N / 8 + 4) * sizeof(typename P::S);
 }
 
 template <class P, int SIGN, int N, int L>
