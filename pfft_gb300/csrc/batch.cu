@@ -102,10 +102,15 @@ Batch* make_batch(Plan* const* plans, int n) {
       // 512 with the same orientation on both sides), else a general tile
       bool ri = false, ro = false;
       long long tiles;
-      if (kernel_path() == 1 && ps.p.N <= 512 && fast::fast_args(bp.p, pl->arith, &bp.fa, &ri, &ro) && ri == ro) {
+      const bool pow2 = !(ps.p.N & (ps.p.N - 1));
+      if (kernel_path() == 1 && ps.p.N <= (pow2 ? 512 : 768) && fast::fast_args(bp.p, pl->arith, &bp.fa, &ri, &ro) &&
+          ri == ro) {
         bp.fastN = ps.p.N;
         bp.frow = ri ? 1 : 0;
-        const int L = batch_fast_lines(bp.fastN);
+        bp.mixed = pow2 ? 0 : 1;
+        // lines per tile: BATCH_THREADS threads of N/8 (radix-8) or N/E (mixed) per line
+        const int L = pow2 ? batch_fast_lines(bp.fastN)
+                           : (pl->arith == ARITH_F32 ? fast::mixed_L<fast::F32>(bp.fastN) : fast::mixed_L<fast::FDD>(bp.fastN));
         tiles = (ps.p.nlines + L - 1) / L;
         const int lsp = fsz == 8 ? bp.fastN + 16 : bp.fastN + bp.fastN / 8 + 4;  // as fast_smem_bytes
         b->smem = std::max(b->smem, (int)(16 * L + (size_t)L * lsp * fsz));

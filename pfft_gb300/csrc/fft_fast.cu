@@ -1,5 +1,6 @@
 // Dispatcher of the register-resident radix-8 pass kernel (fft_fast.cuh).
 #include "fft_fast.cuh"
+#include "fft_mixed.cuh"
 
 namespace pg {
 
@@ -8,7 +9,8 @@ bool fast_args(const PassParams& p, int arith, FastArgs* a, bool* row_in, bool* 
   if (p.mode != MODE_C2C || p.nst == 0) return false;
   if (p.M != p.N || p.Ni != p.N || p.No != p.N || p.Zi || p.Zo || p.wmode) return false;
   const int N = p.N;
-  if (N < 16 || N > 4096 || (N & (N - 1))) return false;
+  const bool pow2 = N >= 16 && N <= 4096 && !(N & (N - 1));
+  if (!pow2 && !mixed_supported(N)) return false;
   if (arith != ARITH_F32 && arith != ARITH_DF) return false;
   if (p.ashI.en || p.ashO.en) return false;
   if (p.nb > PG_MAX_BATCH) return false;
@@ -54,6 +56,18 @@ int launch_fast_pass(const PassParams& p, int arith, cudaStream_t stream) {
   const int N = p.N;
   const bool big = N >= 1024;
   a.fastL = p.fastL;
+  if (N & (N - 1)) {  // 3 * 2^a or 5 * 2^a: mixed-radix kernel
+    const bool three = N % 3 == 0;
+    if (arith == ARITH_F32)
+      return p.sign < 0 ? (three ? launch_mixed_three<F32, -1>(N, a, row_in, row_out, stream)
+                                 : launch_mixed_five<F32, -1>(N, a, row_in, row_out, stream))
+                        : (three ? launch_mixed_three<F32, 1>(N, a, row_in, row_out, stream)
+                                 : launch_mixed_five<F32, 1>(N, a, row_in, row_out, stream));
+    return p.sign < 0 ? (three ? launch_mixed_three<FDD, -1>(N, a, row_in, row_out, stream)
+                               : launch_mixed_five<FDD, -1>(N, a, row_in, row_out, stream))
+                      : (three ? launch_mixed_three<FDD, 1>(N, a, row_in, row_out, stream)
+                               : launch_mixed_five<FDD, 1>(N, a, row_in, row_out, stream));
+  }
   if (arith == ARITH_F32) {
     if (p.sign < 0)
       return big ? launch_large<F32, -1>(N, a, row_in, row_out, stream) : launch_small<F32, -1>(N, a, row_in, row_out, stream);

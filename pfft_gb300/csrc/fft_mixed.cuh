@@ -1,0 +1,323 @@
+// Register-resident mixed-radix pass for c2c lines of 3 * 2^a and 5 * 2^a
+// points (the companion of the radix-8 kernel in fft_fast.cuh).
+//
+// Every thread owns E values of its line (E = 12 for 3 * 2^a lengths, radices
+// 3, 4 and 2; E = 20 for 5 * 2^a with FP32, E = 10 with float-float, radices
+// 5, 4 / 2), N/E threads per line.  The radix schedule is fixed at compile
+// time, so every index of every stage is a constant expression: a stage of
+// radix R runs E/R butterflies per thread, b = t + i * N/E, with inputs
+// x[b + r N/R], twiddles W_{Ns R}^{(b mod Ns) r} and outputs at
+// (b - b mod Ns) R + b mod Ns + r Ns (Stockham autosort).  The first stage
+// loads from global memory, the last stores to global memory (both
+// coalesced as in the radix-8 kernel), the stages in between exchange
+// through one shared-memory buffer.  Same arithmetic policies (F32, FDD), the
+// same tile layout rules (pad, lsp_of) and the same FastArgs.
+#pragma once
+#include "fft_fast.cuh"
+
+namespace pg {
+namespace fast {
+
+// compile-time radix schedule of a length
+template <int N>
+struct MixedSched {
+  static constexpr bool three = N % 3 == 0;
+  static constexpr int E_f32 = three ? 12 : 20;
+  static constexpr int E_dd = three ? 12 : 10;
+  // radix of stage s (0-based): the odd factor first, then 4s, then a 2
+  static constexpr int m2 = three ? N / 3 : N / 5;  // the power of two
+  static constexpr int odd = three ? 3 : 5;
+  static constexpr int log2m = m2 >= 512 ? 9 : m2 >= 256 ? 8 : m2 >= 128 ? 7 : m2 >= 64 ? 6 : m2 >= 32 ? 5
+                               : m2 >= 16 ? 4 : m2 >= 8 ? 3 : m2 >= 4 ? 2 : m2 >= 2 ? 1 : 0;
+  template <int E>
+  __host__ __device__ static constexpr int stages() {
+    // with E = 10 only radix 2 divides E besides 5
+    return E == 10 ? 1 + log2m : 1 + log2m / 2 + (log2m & 1);
+  }
+  template <int E>
+  __host__ __device__ static constexpr int radix(int s) {
+    return s == 0 ? odd : (E == 10 ? 2 : ((log2m & 1) && s == stages<E>() - 1 ? 2 : 4));
+  }
+};
+
+template <class P>
+struct Kc;
+template <>
+struct Kc<F32> {
+  static __device__ __forceinline__ float k(float h, float) { return h; }
+};
+template <>
+struct Kc<FDD> {
+  static __device__ __forceinline__ DD k(float h, float l) { return {h, l}; }
+};
+// a double constant split at compile time into float hi + lo
+#define PG_KC(P, c) Kc<P>::k((float)(c), (float)((c) - (double)(float)(c)))
+
+template <class P, int SIGN>
+__device__ __forceinline__ void bf2(typename P::C* v) {
+  typename P::C a = v[0], b = v[1];
+  v[0] = P::add(a, b);
+  v[1] = P::sub(a, b);
+}
+
+template <class P, int SIGN>
+__device__ __forceinline__ void bf3(typename P::C* v) {
+  typedef typename P::C C;
+  constexpr double S3 = 0.86602540378443864676372317075294;
+  C t = P::add(v[1], v[2]);
+  C u = P::sub(v[1], v[2]);
+  C a0 = v[0];
+  v[0] = P::add(a0, t);
+  C m = P::sub(a0, P::scal(t, PG_KC(P, 0.5)));
+  C su = msi<P, SIGN>(P::scal(u, PG_KC(P, S3)));
+  v[1] = P::add(m, su);
+  v[2] = P::sub(m, su);
+}
+
+template <class P, int SIGN>
+__device__ __forceinline__ void bf5(typename P::C* v) {
+  typedef typename P::C C;
+  constexpr double C1 = 0.30901699437494742410229341718282;   // cos(2 pi / 5)
+  constexpr double C2 = -0.80901699437494742410229341718282;  // cos(4 pi / 5)
+  constexpr double S1 = 0.95105651629515357211643933337938;   // sin(2 pi / 5)
+  constexpr double S2 = 0.58778525229247312916870595463907;   // sin(4 pi / 5)
+  C a0 = v[0];
+  C t1 = P::add(v[1], v[4]), t2 = P::add(v[2], v[3]);
+  C u1 = P::sub(v[1], v[4]), u2 = P::sub(v[2], v[3]);
+  v[0] = P::add(a0, P::add(t1, t2));
+  C m1 = P::add(a0, P::add(P::scal(t1, PG_KC(P, C1)), P::scal(t2, PG_KC(P, C2))));
+  C m2 = P::add(a0, P::add(P::scal(t1, PG_KC(P, C2)), P::scal(t2, PG_KC(P, C1))));
+  C n1 = msi<P, SIGN>(P::add(P::scal(u1, PG_KC(P, S1)), P::scal(u2, PG_KC(P, S2))));
+  C n2 = msi<P, SIGN>(P::sub(P::scal(u1, PG_KC(P, S2)), P::scal(u2, PG_KC(P, S1))));
+  v[1] = P::add(m1, n1);
+  v[4] = P::sub(m1, n1);
+  v[2] = P::add(m2, n2);
+  v[3] = P::sub(m2, n2);
+}
+
+template <class P, int SIGN, int R>
+__device__ __forceinline__ void bfR(typename P::C* v) {
+  if constexpr (R == 2) bf2<P, SIGN>(v);
+  if constexpr (R == 3) bf3<P, SIGN>(v);
+  if constexpr (R == 4) bf4<P, SIGN>(v[0], v[1], v[2], v[3]);
+  if constexpr (R == 5) bf5<P, SIGN>(v);
+}
+
+template <class P>
+__host__ __device__ constexpr int mixed_E(int N) {
+  return sizeof(typename P::S) == 8 ? (N % 3 == 0 ? 12 : 20) : (N % 3 == 0 ? 12 : 10);
+}
+
+// stage s: v holds this stage's inputs (E/R butterflies of R values); run
+// the butterflies, then either store to global (last stage) or exchange
+// through shared memory into the next stage's inputs
+template <class P, int SIGN, int N, int E, int s>
+struct MixedStage {
+  typedef typename P::C C;
+  typedef typename P::S S;
+  static constexpr int NS = MixedSched<N>::template stages<E>();
+  static constexpr int R = MixedSched<N>::template radix<E>(s);
+  static constexpr int TPL = N / E;
+
+  __host__ __device__ static constexpr int ns() {  // product of the radices before stage s
+    int p = 1;
+    for (int q = 0; q < s; q++) p *= MixedSched<N>::template radix<E>(q);
+    return p;
+  }
+
+  // twiddles and butterflies of this stage (inputs in v, outputs in place)
+  static __device__ __forceinline__ void compute(C* v, int t, const S* tw) {
+    constexpr int Ns = ns();
+#pragma unroll
+    for (int i = 0; i < E / R; i++) {
+      const int b = t + i * TPL;
+      if (Ns > 1) {
+        const int k = b % Ns;
+        constexpr int step = N / (Ns * R);
+#pragma unroll
+        for (int r = 1; r < R; r++) v[i * R + r] = P::mul(v[i * R + r], P::twc(__ldg(&tw[k * r * step]), SIGN));
+      }
+      bfR<P, SIGN, R>(v + i * R);
+    }
+  }
+
+  // shared-memory index of output r of butterfly i (natural position)
+  static __device__ __forceinline__ int out_pos(int t, int i, int r) {
+    constexpr int Ns = ns();
+    const int b = t + i * TPL;
+    const int k = b % Ns;
+    return (b - k) * R + k + r * Ns;
+  }
+};
+
+template <class P, int SIGN, int N, int E, int s>
+__device__ __forceinline__ void mixed_stages(typename P::C* v, int t, const typename P::S* tw, typename P::S* line) {
+  typedef MixedStage<P, SIGN, N, E, s> St;
+  St::compute(v, t, tw);
+  if constexpr (s + 1 < St::NS) {
+    // exchange: outputs to shared memory, next stage's inputs back
+    __syncthreads();  // the previous exchange's loads are done
+#pragma unroll
+    for (int i = 0; i < E / St::R; i++)
+#pragma unroll
+      for (int r = 0; r < St::R; r++) line[pad<P>(St::out_pos(t, i, r))] = P::sts(P::renorm(v[i * St::R + r]));
+    __syncthreads();
+    constexpr int R2 = MixedSched<N>::template radix<E>(s + 1);
+#pragma unroll
+    for (int i = 0; i < E / R2; i++)
+#pragma unroll
+      for (int r = 0; r < R2; r++) v[i * R2 + r] = P::lds(line[pad<P>(t + i * (N / E) + r * (N / R2))]);
+    mixed_stages<P, SIGN, N, E, s + 1>(v, t, tw, line);
+  }
+}
+
+// One tile (L lines) of a mixed-radix pass: L * N/E threads.
+template <class P, int SIGN, int N, int L, bool ROW_IN, bool ROW_OUT, bool CG = false>
+__device__ __forceinline__ void mixed_tile(const FastArgs& a, long long blk, unsigned char* sm_raw) {
+  typedef typename P::C C;
+  typedef typename P::S S;
+  typedef typename P::G G;
+  constexpr int E = mixed_E<P>(N);
+  constexpr int TPL = N / E;
+  constexpr int NS = MixedSched<N>::template stages<E>();
+  constexpr int RL = MixedSched<N>::template radix<E>(NS - 1);  // last radix
+  constexpr int R0 = MixedSched<N>::template radix<E>(0);
+  constexpr int LSP = lsp_of<P, N, L, ROW_IN>();
+  long long* offI = (long long*)sm_raw;
+  long long* offO = offI + L;
+  S* buf = (S*)(sm_raw + 16 * L);
+
+  const int tid = threadIdx.x;
+  const long long g0 = blk * L;
+  if (tid < L) {
+    long long g = g0 + tid;
+    if (g >= a.nlines) g = a.nlines - 1;  // tail tile: clamp (duplicate work, never stored)
+    long long oi = 0, oo = 0;
+    for (int b = 0; b < a.nb; b++) {
+      long long e = a.bext[b];
+      long long idx = g % e;
+      g /= e;
+      oi += idx * a.bsI[b];
+      oo += idx * a.bsO[b];
+    }
+    offI[tid] = oi;
+    offO[tid] = oo;
+  }
+  __syncthreads();
+  const int l = ROW_IN ? tid / TPL : tid % L;
+  const int t = ROW_IN ? tid % TPL : tid / L;
+  const bool live = (g0 + l) < a.nlines;
+  const S* tw = (const S*)a.tw;
+  S* line = buf + l * LSP;
+
+  C v[E];
+  {
+    const G* src = (const G*)a.src + offI[l];
+#pragma unroll
+    for (int i = 0; i < E / R0; i++)
+#pragma unroll
+      for (int r = 0; r < R0; r++) {
+        const long long e = t + i * TPL + r * (N / R0);
+        C x = gload<P, CG>(src + e * a.sIa, a.in_df);
+        v[i * R0 + r] = a.conj_in ? P::conj(x) : x;
+      }
+  }
+  mixed_stages<P, SIGN, N, E, 0>(v, t, tw, line);
+  // last stage: output r of butterfly i is element t + i * TPL + r * N/RL
+  if (ROW_IN == ROW_OUT) {
+    if (live) {
+      G* dst = (G*)a.dst + offO[l];
+#pragma unroll
+      for (int i = 0; i < E / RL; i++)
+#pragma unroll
+        for (int r = 0; r < RL; r++) {
+          const long long e = t + i * TPL + r * (N / RL);
+          C o = v[i * RL + r];
+          gstore<P>(dst + e * a.sOa, a.conj_out ? P::conj(o) : o, a.out_df);
+        }
+    }
+    return;
+  }
+  // transposing pass: restage with the output's thread mapping
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < E / RL; i++)
+#pragma unroll
+    for (int r = 0; r < RL; r++) line[pad<P>(t + i * TPL + r * (N / RL))] = P::sts(P::renorm(v[i * RL + r]));
+  __syncthreads();
+  const int l2 = ROW_OUT ? tid / TPL : tid % L;
+  const int t2 = ROW_OUT ? tid % TPL : tid / L;
+  if ((g0 + l2) < a.nlines) {
+    G* d2 = (G*)a.dst + offO[l2];
+    const S* line2 = buf + l2 * LSP;
+#pragma unroll
+    for (int q = 0; q < E; q++) {
+      const int k = t2 + q * TPL;
+      C o = P::lds(line2[pad<P>(k)]);
+      gstore<P>(d2 + (long long)k * a.sOa, a.conj_out ? P::conj(o) : o, a.out_df);
+    }
+  }
+}
+
+template <class P, int SIGN, int N, int L, bool ROW_IN, bool ROW_OUT>
+__global__ void __launch_bounds__(L*(N / mixed_E<P>(N))) k_mixed(const FastArgs a) {
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  mixed_tile<P, SIGN, N, L, ROW_IN, ROW_OUT>(a, blockIdx.x, sm_raw);
+}
+
+template <class P, int N, int L>
+constexpr size_t mixed_smem_bytes() {
+  return 16 * L + (size_t)L * (sizeof(typename P::S) == 8 ? N + 16 : N + N / 8 + 4) * sizeof(typename P::S);
+}
+
+// lines per CTA: about 256 threads
+template <class P>
+__host__ __device__ constexpr int mixed_L(int N) {
+  return 256 / (N / mixed_E<P>(N)) > 0 ? 256 / (N / mixed_E<P>(N)) : 1;
+}
+
+template <class P, int SIGN, int N>
+int launch_mixed_n(const FastArgs& a, bool row_in, bool row_out, cudaStream_t s) {
+  constexpr int L = mixed_L<P>(N);
+  constexpr int T = L * (N / mixed_E<P>(N));
+  const size_t smem = mixed_smem_bytes<P, N, L>();
+  long long grid = (a.nlines + L - 1) / L;
+  if (grid > 2147483647LL) return (int)cudaErrorInvalidConfiguration;
+  cudaError_t e = cudaSuccess;
+#define PG_MIXED_LAUNCH(RI, RO)                                                                            \
+  do {                                                                                                     \
+    static bool attr_done = false;                                                                         \
+    if (!attr_done) {                                                                                      \
+      e = cudaFuncSetAttribute(k_mixed<P, SIGN, N, L, RI, RO>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                               (int)smem);                                                                 \
+      if (e != cudaSuccess) return (int)e;                                                                 \
+      attr_done = true;                                                                                    \
+    }                                                                                                      \
+    k_mixed<P, SIGN, N, L, RI, RO><<<(unsigned)grid, T, smem, s>>>(a);                                     \
+  } while (0)
+  if (row_in && row_out)
+    PG_MIXED_LAUNCH(true, true);
+  else if (!row_in && !row_out)
+    PG_MIXED_LAUNCH(false, false);
+  else if (row_in)
+    PG_MIXED_LAUNCH(true, false);
+  else
+    PG_MIXED_LAUNCH(false, true);
+#undef PG_MIXED_LAUNCH
+  return (int)cudaGetLastError();
+}
+
+// lengths with a mixed-radix kernel
+__host__ __device__ constexpr bool mixed_supported(int N) {
+  return N == 24 || N == 40 || N == 48 || N == 80 || N == 96 || N == 160 || N == 192 || N == 320 || N == 384 ||
+         N == 640 || N == 768;
+}
+
+// launchers, one instantiation set per unit (fft_mixed_<arith>_<dir>_<family>.cu)
+template <class P, int SIGN>
+int launch_mixed_three(int N, const FastArgs& a, bool row_in, bool row_out, cudaStream_t s);
+template <class P, int SIGN>
+int launch_mixed_five(int N, const FastArgs& a, bool row_in, bool row_out, cudaStream_t s);
+
+}  // namespace fast
+}  // namespace pg

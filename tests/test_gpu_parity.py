@@ -162,13 +162,14 @@ def test_double_arith_modes(cuda, pfft_lib):
 
 
 @pytest.mark.parametrize("n,flags", [((32, 32, 32), 0), ((16, 32, 64), TO), ((64, 64, 64), 0), ((128, 64, 256), TO),
-                                     ((512, 8, 16), 0),
+                                     ((96, 48, 40), 0), ((24, 80, 192), TO), ((40, 96, 384), TI), ((768, 6, 160), 0),
+                                     ((8, 640, 320), TO), ((512, 8, 16), 0),
                                      ((16, 1024, 8), TI), ((2048, 4, 4), 0), ((8, 4, 4096), 0)])
 @pytest.mark.parametrize("prec", PRECS)
 def test_kernel_paths_agree(cuda, pfft_lib, n, flags, prec):
-    """The register-resident radix-8 kernel and the general pass kernel both
-    match the oracle on power-of-two c2c lines (row, column and transposing
-    passes, every supported line length)."""
+    """The register-resident radix-8 and mixed-radix (3 * 2^a, 5 * 2^a)
+    kernels and the general pass kernel all match the oracle on c2c lines
+    (row, column and transposing passes, every supported line length)."""
     L = pg.lib()
     try:
         for path in (1, 0):
