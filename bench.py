@@ -329,6 +329,9 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--n", type=int, default=512, help="cube edge (profiling runs use a smaller case)")
     ap.add_argument("--shape", default=None, help="n0xn1xn2 instead of a cube (profiling runs)")
+    ap.add_argument("--export-wisdom", default=None, help="write the planner's wisdom to this file after planning")
+    ap.add_argument("--import-wisdom", default=None,
+                    help="load wisdom from this file and plan with PFFT_MEASURE (the recorded choices, no timing)")
     ap.add_argument("--no-tune", action="store_true",
                     help="plan with PFFT_MEASURE instead of PFFT_PATIENT (by default the autotuner times every "
                          "pass's candidates at planning time, before the timed region)")
@@ -357,10 +360,16 @@ def main():
     a = host.to(dev)
     b = torch.empty_like(a)
     comm = pg.procmesh(2)
+    if args.import_wisdom:
+        if L.pfft_gb300_import_wisdom_from_filename(args.import_wisdom.encode()) != 1:
+            raise RuntimeError("cannot import wisdom from %s" % args.import_wisdom)
+        args.no_tune = True
     plan_flags = pg.PFFT_TRANSPOSED_NONE | (pg.PFFT_MEASURE if args.no_tune else pg.PFFT_PATIENT)
     plan = getattr(L, pre + "plan_dft_3d")(pg.ints(n), a.data_ptr(), b.data_ptr(), comm, pg.PFFT_FORWARD, plan_flags)
     if not plan:
         raise RuntimeError("plan failed: %s" % (pg.last_error(),))
+    if args.export_wisdom:
+        L.pfft_gb300_export_wisdom_to_filename(args.export_wisdom.encode())
     stream = torch.cuda.Stream(device=dev)
     getattr(L, pre + "gb300_set_stream")(plan, ctypes.c_void_p(stream.cuda_stream))
     getattr(L, pre + "gb300_set_sync")(plan, 0)
@@ -452,7 +461,8 @@ def main():
         "config": {"workload": "pfft_execute c2c %s %s forward, 1x1 procmesh, out-of-place, "
                                "TRANSPOSED_NONE" % ("x".join(map(str, n)) if args.shape else "%d^3" % args.n,
                                                     "complex128" if args.prec == "double" else "complex64"),
-                   "bytes_per_step": B, "p_min": pmin, "planner": "PFFT_MEASURE" if args.no_tune else "PFFT_PATIENT (autotuned at planning time)",
+                   "bytes_per_step": B, "p_min": pmin, "planner": ("PFFT_MEASURE with imported wisdom" if args.import_wisdom else "PFFT_MEASURE") if args.no_tune
+                   else "PFFT_PATIENT (autotuned at planning time)",
                    "l2": "arrays (%.2f GB each) larger than the 129 MB L2; no flush" % (cnt * esz / 1e9),
                    "parallelism": "replicas" if world > 1
                    else "single GPU"},
