@@ -97,3 +97,53 @@ def test_batch_wait_is_bounded(cuda, pfft_lib):
     assert L.pfft_gb300_batch_wait_selftest(1000) == -2
     x = torch.ones(4, device="cuda")
     assert float(x.sum()) == 4.0
+
+
+@pytest.mark.parametrize("prec,tol", [("double", 1e-12), ("float", 2e-6)])
+def test_batch_mixed_plan_kinds(cuda, pfft_lib, prec, tol):
+    """One batch of r2c (padded, transposed out), c2r, r2r and c2c plans of
+    different shapes: every output matches the oracle."""
+    from tests.pfft_util import mask_padding, random_input
+    torch = cuda
+    L = pg.lib()
+    pre = "pfftf_" if prec == "float" else "pfft_"
+    rdt = torch.float32 if prec == "float" else torch.float64
+    TO, PAD = pg.PFFT_TRANSPOSED_OUT, pg.PFFT_PADDED_R2C
+    reqs = [Req("r2c", (32, 48, 64), flags=PAD | TO), Req("c2r", (40, 24, 32), sign=1),
+            Req("r2r", (24, 20, 18), kinds=[5, 4, 7]), Req("c2c", (96, 32, 40), flags=TO),
+            Req("c2c", (128, 16, 64), sign=1)]
+    names = {"c2c": "plan_many_dft", "r2c": "plan_many_dft_r2c", "c2r": "plan_many_dft_c2r", "r2r": "plan_many_r2r"}
+    rng = np.random.default_rng(9)
+    comm = pg.procmesh(2)
+    plans, keep = [], []
+    for req in reqs:
+        ci, co, mem = req.counts()
+        words = max(2 * mem, ci, co)
+        x = random_input(req, rng)
+        if prec == "float":
+            x = x.astype(np.float32).astype(np.float64)
+        a = torch.zeros(words, dtype=rdt, device="cuda")
+        b = torch.zeros(words, dtype=rdt, device="cuda")
+        a[:ci] = torch.from_numpy(x).to("cuda", rdt)
+        fn = getattr(L, pre + names[req.kind])
+        n, ni, no = pg.ints(req.n), pg.ints(req.ni), pg.ints(req.no)
+        if req.kind == "r2r":
+            p = fn(req.d, n, ni, no, 1, None, None, a.data_ptr(), b.data_ptr(), comm, pg.cints(req.kinds), req.flags)
+        else:
+            p = fn(req.d, n, ni, no, 1, None, None, a.data_ptr(), b.data_ptr(), comm, req.sign, req.flags)
+        assert p, pg.last_error()
+        plans.append(p)
+        keep.append((req, x, a, b, co))
+    arr = (ctypes.c_void_p * len(plans))(*plans)
+    bt = getattr(L, pre + "gb300_batch_create")(len(plans), arr)
+    assert bt, pg.last_error()
+    try:
+        assert L.pfft_gb300_batch_execute(bt) == 0
+        for req, x, a, b, co in keep:
+            got = mask_padding(req, b[:co].double().cpu().numpy())
+            ref = mask_padding(req, oracle_run(req, x))
+            assert rel_l2(got, ref) <= tol, req.kind
+    finally:
+        L.pfft_gb300_batch_destroy(bt)
+        for p in plans:
+            getattr(L, pre + "destroy_plan")(p)
