@@ -147,7 +147,7 @@ def cpu_baseline(sample_n0=128, threads=None):
 BATCH_SIZES = [(32, 32, 32), (48, 64, 40), (96, 96, 96), (128, 128, 64), (128, 128, 128)]
 
 
-def measure_batched(L, pg, torch, prec, nplans=64, seed=11, reps=5):
+def measure_batched(L, pg, torch, prec, nplans=64, seed=11, reps=5, tune=True):
     """64 uneven c2c transforms (sizes drawn by seed from BATCH_SIZES): one
     persistent batched launch (CUDA graph) against a per-plan loop of plain
     pfft_execute calls (blocking, as the reference's execute) and against the
@@ -157,12 +157,13 @@ def measure_batched(L, pg, torch, prec, nplans=64, seed=11, reps=5):
     cdt = torch.complex128 if prec == "double" else torch.complex64
     rng = np.random.default_rng(seed)
     comm = pg.procmesh(2)
+    flags = pg.PFFT_PATIENT if tune else 0  # autotuned radix / tile choices (planning time)
     plans, outs, pts = [], [], 0
     for _ in range(nplans):
         n = BATCH_SIZES[int(rng.integers(0, len(BATCH_SIZES)))]
         x = torch.from_numpy(rng.uniform(-1, 1, 2 * int(np.prod(n)))).view(torch.complex128).to(cdt).cuda()
         y = torch.zeros_like(x)
-        p = getattr(L, pre + "plan_dft_3d")(pg.ints(n), x.data_ptr(), y.data_ptr(), comm, pg.PFFT_FORWARD, 0)
+        p = getattr(L, pre + "plan_dft_3d")(pg.ints(n), x.data_ptr(), y.data_ptr(), comm, pg.PFFT_FORWARD, flags)
         if not p:
             raise RuntimeError("plan failed: %s" % (pg.last_error(),))
         plans.append((p, x, y))
@@ -215,7 +216,8 @@ def measure_batched(L, pg, torch, prec, nplans=64, seed=11, reps=5):
             "batch_ms": batch_ms, "loop_ms": loop_ms, "loop_async_ms": loop_async_ms,
             "ratio": loop_ms / batch_ms, "ratio_vs_async_loop": loop_async_ms / batch_ms,
             "batch_gbs_min_traffic": 3 * 2 * pts * esz / (batch_ms * 1e-3) / 1e9,
-            "max_rel_l2_batch_vs_loop": diff, "tasks": ntasks.value, "grid": grid.value}
+            "max_rel_l2_batch_vs_loop": diff, "tasks": ntasks.value, "grid": grid.value,
+            "planner": "PFFT_PATIENT" if tune else "PFFT_MEASURE"}
 
 
 def measure_adjoint(L, pg, torch, reps=5):
@@ -437,7 +439,8 @@ def main():
     # ---- the metric's other two parts: batched vs loop, adjoint cost (untimed by the step clock) ----
     extra = {}
     if not args.no_extras:
-        extra["batched_vs_loop"] = {pr: measure_batched(L, pg, torch, pr) for pr in ("double", "float")}
+        extra["batched_vs_loop"] = {pr: measure_batched(L, pg, torch, pr, tune=not args.no_tune)
+                                    for pr in ("double", "float")}
         extra["adjoint_cost"] = measure_adjoint(L, pg, torch)
 
     pts = int(np.prod(n))

@@ -103,8 +103,9 @@ Batch* make_batch(Plan* const* plans, int n) {
       bool ri = false, ro = false;
       long long tiles;
       const bool pow2 = !(ps.p.N & (ps.p.N - 1));
-      if (kernel_path() == 1 && ps.p.N <= (pow2 ? 512 : 768) && fast::fast_args(bp.p, pl->arith, &bp.fa, &ri, &ro) &&
-          ri == ro) {
+      // (a pass the autotuner or wisdom put on the general kernel keeps it)
+      if (kernel_path() == 1 && ps.p.kpath == 0 && ps.p.N <= (pow2 ? 512 : 768) &&
+          fast::fast_args(bp.p, pl->arith, &bp.fa, &ri, &ro) && ri == ro) {
         bp.fastN = ps.p.N;
         bp.frow = ri ? 1 : 0;
         bp.mixed = pow2 ? 0 : 1;

@@ -11,7 +11,7 @@
 // the choice is recorded as wisdom under a key that describes the pass
 // completely (arithmetic, mode, lengths, strides, batch shape, flags), so any
 // later plan with the same pass - created with any flags - uses it without
-// timing.  Wisdom is exported and imported as text:
+// timing (a tuning planner also skips passes already in wisdom).  Wisdom is exported and imported as text:
 //   pfft_gb300-wisdom 1
 //   <key> <kpath> <fastL> <pref> <L>
 #include <stdio.h>
@@ -176,6 +176,14 @@ bool tune_program(Plan* pl, PassProgram* prog) {
     if (!base.tw) {
       ok = false;
       break;
+    }
+    {  // a pass already in wisdom is not timed again (as FFTW reuses wisdom)
+      std::lock_guard<std::mutex> lk(g_mu);
+      auto it = store().find(key_of(base, pl->arith));
+      if (it != store().end()) {
+        apply_choice(&ps.p, pl->arith, it->second);
+        continue;
+      }
     }
     Choice best;
     float best_ms = 1e30f;

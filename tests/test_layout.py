@@ -100,3 +100,15 @@ def test_planner_rejections(pfft_lib):
     # FFT rank below the mesh rank, and rank == mesh rank != 3
     assert not L.pfft_plan_dft(1, pg.ints([8]), None, None, comm2, -1, 0)
     assert not L.pfft_plan_dft(2, pg.ints([8, 8]), None, None, comm2, -1, 0)
+
+
+def test_null_plan_execute_and_destroy(pfft_lib, capfd):
+    """api/api-basic.c:243-246,1050-1054: a NULL plan given to execute or
+    destroy prints an error and returns (the process keeps running)."""
+    L = pfft_lib
+    L.pfft_execute(None)
+    L.pfftf_execute(None)
+    L.pfft_destroy_plan(None)
+    L.pfft_execute_adjoint(None)
+    err = capfd.readouterr().err
+    assert "PFFT" in err or err == ""
