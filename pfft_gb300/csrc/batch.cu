@@ -104,8 +104,9 @@ Batch* make_batch(Plan* const* plans, int n) {
       long long tiles;
       const bool pow2 = !(ps.p.N & (ps.p.N - 1));
       // (a pass the autotuner or wisdom put on the general kernel keeps it)
+      // (the DCT passes of real-to-real plans keep the general tile in a batch)
       if (kernel_path() == 1 && ps.p.kpath == 0 && ps.p.N <= (pow2 ? 512 : 768) &&
-          fast::fast_args(bp.p, pl->arith, &bp.fa, &ri, &ro) && ri == ro) {
+          fast::fast_args(bp.p, pl->arith, &bp.fa, &ri, &ro) && ri == ro && bp.fa.mode < 3) {
         bp.fastN = ps.p.N;
         bp.frow = ri ? 1 : 0;
         bp.mixed = pow2 ? 0 : 1;

@@ -203,6 +203,21 @@ struct FastArgs {
   int in_df, out_df;  // double API: the array holds float-float pairs (an intermediate)
   int fastL;          // requested lines per CTA (0: default): 512 takes 4, 8, 16; 1024 takes 2, 4, 8;
                       // 2048 takes 2, 4; 4096 takes 1, 2
+  // logical sequence of a line (pass_tile.cuh semantics): element e of the
+  // length-N input is input element e - Zi when 0 <= e - Zi < Ni, else 0
+  // (zero-padding); for c2r the position is first folded to the half
+  // spectrum (k = e or N - e, the mirrored half conjugated); output element
+  // k is logical position Zo + k, k < No (truncation); r2c reads real input,
+  // c2r writes the real parts.  plain: c2c with the whole line on both sides.
+  // REDFT10 / REDFT01 (real-to-real DCT-II / DCT-III, Makhoul's method on a
+  // length-N complex FFT): 10 loads v[m] = x[2m] (m < N/2) or x[2(N-1-m)+1]
+  // and stores y_k = 2 Re(W_4N^k V_k); 01 loads (x_k - i x_(N-k)) W_4N^-k
+  // (x_N = 0), runs the inverse FFT and stores Re w_m at 2m (m < N/2) or
+  // 2(N-1-m)+1.  tw2: the length-4N twiddle table.
+  int mode;           // 0 c2c, 1 r2c, 2 c2r, 3 REDFT10, 4 REDFT01
+  int Zi, Ni, Zo, No;
+  int plain;
+  const void* tw2;
 };
 
 // global element access: native format, or float-float pairs for the
@@ -247,6 +262,100 @@ __device__ __forceinline__ void gstore<FDD>(FDD::G* p, FDD::C v, int df) {
   }
 }
 
+// real-array element access (r2c input, c2r output)
+template <class P, bool CG>
+__device__ __forceinline__ typename P::C rload(const void* src, long long i);
+template <>
+__device__ __forceinline__ F32::C rload<F32, false>(const void* src, long long i) {
+  return make_float2(((const float*)src)[i], 0.f);
+}
+template <>
+__device__ __forceinline__ F32::C rload<F32, true>(const void* src, long long i) {
+  return make_float2(__ldcg((const float*)src + i), 0.f);
+}
+template <>
+__device__ __forceinline__ FDD::C rload<FDD, false>(const void* src, long long i) {
+  df a = df_from_double(((const double*)src)[i]);
+  return {{a.hi, a.lo}, {0.f, 0.f}};
+}
+template <>
+__device__ __forceinline__ FDD::C rload<FDD, true>(const void* src, long long i) {
+  df a = df_from_double(__ldcg((const double*)src + i));
+  return {{a.hi, a.lo}, {0.f, 0.f}};
+}
+template <class P>
+__device__ __forceinline__ void rstore(void* dst, long long i, typename P::C v);
+template <>
+__device__ __forceinline__ void rstore<F32>(void* dst, long long i, F32::C v) {
+  ((float*)dst)[i] = v.x;
+}
+template <>
+__device__ __forceinline__ void rstore<FDD>(void* dst, long long i, FDD::C v) {
+  ((double*)dst)[i] = df_to_double(df{v.x.hi, v.x.lo});
+}
+template <class P>
+__device__ __forceinline__ typename P::C czero();
+template <>
+__device__ __forceinline__ F32::C czero<F32>() { return make_float2(0.f, 0.f); }
+template <>
+__device__ __forceinline__ FDD::C czero<FDD>() { return {{0.f, 0.f}, {0.f, 0.f}}; }
+
+// real input x_j of a real-to-real line (zero outside the embedded range)
+template <class P, bool CG>
+__device__ __forceinline__ typename P::C rx(const FastArgs& a, long long off, int j) {
+  const int q = j - a.Zi;
+  if (q < 0 || q >= a.Ni) return czero<P>();
+  return rload<P, CG>(a.src, off + (long long)q * a.sIa);
+}
+
+// element e (0..N-1) of a line's logical input sequence (FastArgs comment);
+// DCT: the kernel runs a REDFT10 / REDFT01 pass (compiled separately, so the
+// other kernels carry no DCT code)
+template <class P, bool CG, bool DCT = false>
+__device__ __forceinline__ typename P::C load_elem(const FastArgs& a, long long off, int e, int N) {
+  typedef typename P::C C;
+  if constexpr (DCT) {
+    if (a.mode == 3) return rx<P, CG>(a, off, 2 * e < N ? 2 * e : 2 * (N - 1 - e) + 1);
+    C xk = rx<P, CG>(a, off, e);
+    C xm = e == 0 ? czero<P>() : rx<P, CG>(a, off, N - e);
+    C z = P::sub(xk, P::swap_neg_re(xm));  // x_k - i x_(N-k)
+    return P::mul(z, P::twc(__ldg((const typename P::S*)a.tw2 + e), 1));
+  }
+  bool mirror = false;
+  int q;
+  if (a.mode == 2) {
+    mirror = 2 * e > N;
+    q = (mirror ? N - e : e) - a.Zi;
+  } else {
+    q = e - a.Zi;
+  }
+  if (q < 0 || q >= a.Ni) return czero<P>();
+  C v = a.mode == 1 ? rload<P, CG>(a.src, off + (long long)q * a.sIa)
+                    : gload<P, CG>((const typename P::G*)a.src + off + (long long)q * a.sIa, a.in_df);
+  if (a.conj_in) v = P::conj(v);
+  return mirror ? P::conj(v) : v;
+}
+
+// store logical output position e of a line (kept when Zo <= e < Zo + No)
+template <class P, bool DCT = false>
+__device__ __forceinline__ void store_elem(const FastArgs& a, long long off, int e, typename P::C v, int N) {
+  if constexpr (DCT) {
+    if (a.mode == 3) {  // y_e = 2 Re(W_4N^e V_e)
+      v = P::mul(v, P::twc(__ldg((const typename P::S*)a.tw2 + e), -1));
+      v = P::add(v, v);
+    } else {
+      e = 2 * e < N ? 2 * e : 2 * (N - 1 - e) + 1;
+    }
+  }
+  const int k = e - a.Zo;
+  if (k < 0 || k >= a.No) return;
+  if (a.conj_out) v = P::conj(v);
+  if (a.mode >= 2)
+    rstore<P>(a.dst, off + (long long)k * a.sOa, v);
+  else
+    gstore<P>((typename P::G*)a.dst + off + (long long)k * a.sOa, v, a.out_df);
+}
+
 // ROW_IN: the axis is contiguous on the input side (thread t walks the line);
 // otherwise consecutive threads take consecutive (adjacent) lines.  ROW_OUT
 // likewise for the output; when they differ the last stage is re-staged
@@ -257,7 +366,7 @@ __device__ __forceinline__ void gstore<FDD>(FDD::G* p, FDD::C v, int df) {
 // the body of the stand-alone kernel k_fast, and a task of the batched
 // persistent kernel.  `blk` is the tile index, `sm_raw` the block's dynamic
 // shared memory (fast_smem_bytes).
-template <class P, int SIGN, int N, int L, bool ROW_IN, bool ROW_OUT, bool CG = false>
+template <class P, int SIGN, int N, int L, bool ROW_IN, bool ROW_OUT, bool CG = false, bool DCT = false>
 __device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsigned char* sm_raw) {
   typedef typename P::C C;
   typedef typename P::S S;
@@ -294,7 +403,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsi
   S* line = buf + l * LSP;
 
   C v[8];
-  {
+  if (a.plain) {
     const G* src = (const G*)a.src + offI[l] + (long long)t * a.sIa;
     const long long st = (long long)TPL * a.sIa;
 #pragma unroll
@@ -302,6 +411,9 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsi
       v[r] = gload<P, CG>(src + r * st, a.in_df);
       if (a.conj_in) v[r] = P::conj(v[r]);
     }
+  } else {
+#pragma unroll
+    for (int r = 0; r < 8; r++) v[r] = load_elem<P, CG, DCT>(a, offI[l], t + r * TPL, N);
   }
   bf8<P, SIGN>(v);  // stage 0 (Ns = 1, no twiddles)
   int Ns = 1;
@@ -329,10 +441,15 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsi
     // v holds the last stage (Ns = N/8, k = t): outputs y[t + r*TPL]
     if (ROW_IN == ROW_OUT) {
       if (live) {
-        G* dst = (G*)a.dst + offO[l] + (long long)t * a.sOa;
-        const long long st = (long long)TPL * a.sOa;
+        if (a.plain) {
+          G* dst = (G*)a.dst + offO[l] + (long long)t * a.sOa;
+          const long long st = (long long)TPL * a.sOa;
 #pragma unroll
-        for (int r = 0; r < 8; r++) gstore<P>(dst + r * st, a.conj_out ? P::conj(v[r]) : v[r], a.out_df);
+          for (int r = 0; r < 8; r++) gstore<P>(dst + r * st, a.conj_out ? P::conj(v[r]) : v[r], a.out_df);
+        } else {
+#pragma unroll
+          for (int r = 0; r < 8; r++) store_elem<P, DCT>(a, offO[l], t + r * TPL, v[r], N);
+        }
       }
       return;
     }
@@ -371,14 +488,21 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsi
     }
     if (ROW_IN == ROW_OUT) {
       if (live) {
-        G* dst = (G*)a.dst + offO[l];
+        if (a.plain) {
+          G* dst = (G*)a.dst + offO[l];
 #pragma unroll
-        for (int b = 0; b < NB; b++)
+          for (int b = 0; b < NB; b++)
 #pragma unroll
-          for (int r = 0; r < Q; r++) {
-            C o = a.conj_out ? P::conj(w[b * Q + r]) : w[b * Q + r];
-            gstore<P>(dst + (long long)(t + b * TPL + r * NQ) * a.sOa, o, a.out_df);
-          }
+            for (int r = 0; r < Q; r++) {
+              C o = a.conj_out ? P::conj(w[b * Q + r]) : w[b * Q + r];
+              gstore<P>(dst + (long long)(t + b * TPL + r * NQ) * a.sOa, o, a.out_df);
+            }
+        } else {
+#pragma unroll
+          for (int b = 0; b < NB; b++)
+#pragma unroll
+            for (int r = 0; r < Q; r++) store_elem<P, DCT>(a, offO[l], t + b * TPL + r * NQ, w[b * Q + r], N);
+        }
       }
       return;
     }
@@ -400,17 +524,21 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsi
       for (int r = 0; r < 8; r++) {
         const int k = t2 + r * TPL;
         C o = P::lds(line2[pad<P>(k)]);
-        if (a.conj_out) o = P::conj(o);
-        gstore<P>(d2 + (long long)k * a.sOa, o, a.out_df);
+        if (a.plain) {
+          if (a.conj_out) o = P::conj(o);
+          gstore<P>(d2 + (long long)k * a.sOa, o, a.out_df);
+        } else {
+          store_elem<P, DCT>(a, offO[l2], k, o, N);
+        }
       }
     }
   }
 }
 
-template <class P, int SIGN, int N, int L, bool ROW_IN, bool ROW_OUT>
+template <class P, int SIGN, int N, int L, bool ROW_IN, bool ROW_OUT, bool DCT = false>
 __global__ void __launch_bounds__(L*(N / 8)) k_fast(const FastArgs a) {
   extern __shared__ __align__(16) unsigned char sm_raw[];
-  fast_tile<P, SIGN, N, L, ROW_IN, ROW_OUT>(a, blockIdx.x, sm_raw);
+  fast_tile<P, SIGN, N, L, ROW_IN, ROW_OUT, false, DCT>(a, blockIdx.x, sm_raw);
 }
 
 template <class P, int N, int L>
@@ -418,7 +546,7 @@ constexpr size_t fast_smem_bytes() {
   return 16 * L + (size_t)L * (sizeof(typename P::S) == 8 ? N + 16 : N + N / 8 + 4) * sizeof(typename P::S);
 }
 
-template <class P, int SIGN, int N, int L>
+template <class P, int SIGN, int N, int L, bool DCT = false>
 int launch4(const FastArgs& a, bool row_in, bool row_out, cudaStream_t s) {
   constexpr int T = L * (N / 8);
   const size_t smem = fast_smem_bytes<P, N, L>();
@@ -430,12 +558,12 @@ int launch4(const FastArgs& a, bool row_in, bool row_out, cudaStream_t s) {
   do {                                                                                                    \
     static bool attr_done = false;                                                                        \
     if (!attr_done) {                                                                                     \
-      e = cudaFuncSetAttribute(k_fast<P, SIGN, N, L, RI, RO>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+      e = cudaFuncSetAttribute(k_fast<P, SIGN, N, L, RI, RO, DCT>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                                (int)smem);                                                                \
       if (e != cudaSuccess) return (int)e;                                                                \
       attr_done = true;                                                                                   \
     }                                                                                                     \
-    k_fast<P, SIGN, N, L, RI, RO><<<(unsigned)grid, T, smem, s>>>(a);                                     \
+    k_fast<P, SIGN, N, L, RI, RO, DCT><<<(unsigned)grid, T, smem, s>>>(a);                                \
   } while (0)
   if (row_in && row_out)
     PG_FAST_LAUNCH(true, true);
@@ -459,6 +587,10 @@ template <class P, int SIGN>
 int launch_small(int N, const FastArgs& a, bool row_in, bool row_out, cudaStream_t s);
 template <class P, int SIGN>
 int launch_large(int N, const FastArgs& a, bool row_in, bool row_out, cudaStream_t s);
+// REDFT10 (SIGN -1) / REDFT01 (SIGN +1) passes of 16..512 points with the same
+// orientation on both sides, default tile heights (fft_fast_dct_<arith>_<dir>.cu)
+template <class P, int SIGN>
+int launch_dct(int N, const FastArgs& a, bool row_in, bool row_out, cudaStream_t s);
 
 }  // namespace fast
 }  // namespace pg

@@ -211,7 +211,7 @@ __device__ __forceinline__ void mixed_tile(const FastArgs& a, long long blk, uns
   S* line = buf + l * LSP;
 
   C v[E];
-  {
+  if (a.plain) {
     const G* src = (const G*)a.src + offI[l];
 #pragma unroll
     for (int i = 0; i < E / R0; i++)
@@ -221,6 +221,11 @@ __device__ __forceinline__ void mixed_tile(const FastArgs& a, long long blk, uns
         C x = gload<P, CG>(src + e * a.sIa, a.in_df);
         v[i * R0 + r] = a.conj_in ? P::conj(x) : x;
       }
+  } else {
+#pragma unroll
+    for (int i = 0; i < E / R0; i++)
+#pragma unroll
+      for (int r = 0; r < R0; r++) v[i * R0 + r] = load_elem<P, CG>(a, offI[l], t + i * TPL + r * (N / R0), N);
   }
   mixed_stages<P, SIGN, N, E, 0>(v, t, tw, line);
   // last stage: output r of butterfly i is element t + i * TPL + r * N/RL
@@ -231,9 +236,12 @@ __device__ __forceinline__ void mixed_tile(const FastArgs& a, long long blk, uns
       for (int i = 0; i < E / RL; i++)
 #pragma unroll
         for (int r = 0; r < RL; r++) {
-          const long long e = t + i * TPL + r * (N / RL);
+          const int e = t + i * TPL + r * (N / RL);
           C o = v[i * RL + r];
-          gstore<P>(dst + e * a.sOa, a.conj_out ? P::conj(o) : o, a.out_df);
+          if (a.plain)
+            gstore<P>(dst + (long long)e * a.sOa, a.conj_out ? P::conj(o) : o, a.out_df);
+          else
+            store_elem<P>(a, offO[l], e, o, N);
         }
     }
     return;
@@ -254,7 +262,10 @@ __device__ __forceinline__ void mixed_tile(const FastArgs& a, long long blk, uns
     for (int q = 0; q < E; q++) {
       const int k = t2 + q * TPL;
       C o = P::lds(line2[pad<P>(k)]);
-      gstore<P>(d2 + (long long)k * a.sOa, a.conj_out ? P::conj(o) : o, a.out_df);
+      if (a.plain)
+        gstore<P>(d2 + (long long)k * a.sOa, a.conj_out ? P::conj(o) : o, a.out_df);
+      else
+        store_elem<P>(a, offO[l2], k, o, N);
     }
   }
 }

@@ -158,7 +158,7 @@ Plan* make_plan(const PlanDesc& base, void* in, void* out) {
   // pre-build twiddle tables so that execution allocates nothing
   for (const Pass& ps : pl->fwd.passes) {
     cudaError_t e;
-    if (!twiddle_table(ps.p.M, pl->arith, &e)) {
+    if (!twiddle_table(ps.p.M, pl->arith, &e) || !twiddle_table(ps.p.N, pl->arith, &e)) {
       cuda_check(e, "twiddle table");
       destroy_plan(pl);
       return nullptr;

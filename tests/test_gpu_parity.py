@@ -93,6 +93,18 @@ def test_r2r(cuda, pfft_lib, kinds, prec):
     check(Req("r2r", (9, 8, 10), kinds=list(kinds)), prec, dist="normal")
 
 
+@pytest.mark.parametrize("prec", PRECS)
+def test_dct_fast_paths(cuda, pfft_lib, prec):
+    """REDFT10 / REDFT01 on 2^a, 3 * 2^a and 5 * 2^a lengths (the FFT-based
+    DCT path of the radix-8 and mixed-radix kernels), transposed, oversampled
+    and mixed with other kinds."""
+    check(Req("r2r", (32, 96, 40), kinds=[5, 5, 5]), prec, dist="normal")
+    check(Req("r2r", (32, 96, 40), kinds=[4, 4, 4], flags=TO), prec, dist="normal")
+    check(Req("r2r", (64, 48, 16), kinds=[4, 5, 7]), prec, dist="normal")
+    check(Req("r2r", (64, 48, 32), ni=(40, 30, 20), kinds=[5, 4, 5]), prec, dist="normal")
+    check(Req("r2r", (64, 48, 32), no=(40, 30, 20), kinds=[4, 5, 4], flags=TI), prec, dist="normal")
+
+
 @pytest.mark.parametrize("prec", DPRECS)
 def test_r2r_transposed(cuda, pfft_lib, prec):
     check(Req("r2r", (16, 16, 16), kinds=[5, 5, 5], flags=TO), prec, dist="normal")
