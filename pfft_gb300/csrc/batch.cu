@@ -98,15 +98,16 @@ Batch* make_batch(Plan* const* plans, int n) {
         return nullptr;
       }
       bp.done = (int)hp.size();
-      // radix-8 tile when the pass qualifies (power-of-two c2c lines up to
-      // 512 with the same orientation on both sides), else a general tile
+      // radix-8 / mixed-radix tile when the pass qualifies (plain c2c lines
+      // of up to 512 (2^a) or 768 (3 * 2^a, 5 * 2^a) points with the same
+      // orientation on both sides), else a general tile
       bool ri = false, ro = false;
       long long tiles;
       const bool pow2 = !(ps.p.N & (ps.p.N - 1));
       // (a pass the autotuner or wisdom put on the general kernel keeps it)
-      // (the DCT passes of real-to-real plans keep the general tile in a batch)
+      // (r2c / c2r / windowed / DCT passes keep the general tile in a batch)
       if (kernel_path() == 1 && ps.p.kpath == 0 && ps.p.N <= (pow2 ? 512 : 768) &&
-          fast::fast_args(bp.p, pl->arith, &bp.fa, &ri, &ro) && ri == ro && bp.fa.mode < 3) {
+          fast::fast_args(bp.p, pl->arith, &bp.fa, &ri, &ro) && ri == ro && bp.fa.plain) {
         bp.fastN = ps.p.N;
         bp.frow = ri ? 1 : 0;
         bp.mixed = pow2 ? 0 : 1;

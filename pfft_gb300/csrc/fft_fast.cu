@@ -9,10 +9,13 @@ namespace fast {
 bool fast_args(const PassParams& p, int arith, FastArgs* a, bool* row_in, bool* row_out) {
   const bool dct = p.mode == MODE_RE10 || p.mode == MODE_RE01;
   if ((p.mode != MODE_C2C && p.mode != MODE_R2C && p.mode != MODE_C2R && !dct) || p.nst == 0) return false;
-  if (p.M != (dct ? 4 * p.N : p.N) || p.Ni > p.N || p.No > p.N || p.wmode) return false;
+  if (p.M != (dct ? 4 * p.N : p.N) || p.Ni > p.N || p.No > p.N) return false;
+  if (p.wmode && !((p.wmode == 1 && p.mode == MODE_C2R) || (p.wmode == 2 && p.mode == MODE_R2C))) return false;
   const int N = p.N;
   const bool pow2 = N >= 16 && N <= 4096 && !(N & (N - 1));
-  if (!pow2 && (!mixed_supported(N) || p.mode == MODE_RE10 || p.mode == MODE_RE01)) return false;
+  const bool plain = p.mode == MODE_C2C && p.Zi == 0 && p.Ni == N && p.Zo == 0 && p.No == N && !p.wmode;
+  // the mixed-radix kernel reads and writes plain c2c lines only
+  if (!pow2 && (!mixed_supported(N) || !plain)) return false;
   if ((p.mode == MODE_RE10 || p.mode == MODE_RE01) && N > 512) return false;
   if (arith != ARITH_F32 && arith != ARITH_DF) return false;
   if (p.ashI.en || p.ashO.en) return false;
@@ -47,7 +50,8 @@ bool fast_args(const PassParams& p, int arith, FastArgs* a, bool* row_in, bool* 
   a->Ni = p.Ni;
   a->Zo = p.Zo;
   a->No = p.No;
-  a->plain = (a->mode == 0 && p.Zi == 0 && p.Ni == p.N && p.Zo == 0 && p.No == p.N) ? 1 : 0;
+  a->plain = plain ? 1 : 0;
+  a->wmode = p.wmode;
   *row_in = p.sIa == 1;
   *row_out = p.sOa == 1;
   // column mapping needs adjacent lines on that side
@@ -92,6 +96,11 @@ int launch_fast_pass(const PassParams& p, int arith, cudaStream_t stream) {
                       : (three ? launch_mixed_three<FDD, 1>(N, a, row_in, row_out, stream)
                                : launch_mixed_five<FDD, 1>(N, a, row_in, row_out, stream));
   }
+  if (!a.plain)  // r2c / c2r / windows / weights: the general-I/O instantiations
+    return arith == ARITH_F32 ? (sign < 0 ? launch_gio<F32, -1>(N, a, row_in, row_out, stream)
+                                          : launch_gio<F32, 1>(N, a, row_in, row_out, stream))
+                              : (sign < 0 ? launch_gio<FDD, -1>(N, a, row_in, row_out, stream)
+                                          : launch_gio<FDD, 1>(N, a, row_in, row_out, stream));
   if (arith == ARITH_F32) {
     if (sign < 0)
       return big ? launch_large<F32, -1>(N, a, row_in, row_out, stream) : launch_small<F32, -1>(N, a, row_in, row_out, stream);

@@ -123,6 +123,20 @@ struct FDD {
   }
 };
 
+// constants of a policy: a double split at compile time into float hi + lo
+template <class P>
+struct Kc;
+template <>
+struct Kc<F32> {
+  static __device__ __forceinline__ float k(float h, float) { return h; }
+};
+template <>
+struct Kc<FDD> {
+  static __device__ __forceinline__ DD k(float h, float l) { return {h, l}; }
+};
+// a double constant split at compile time into float hi + lo
+#define PG_KC(P, c) Kc<P>::k((float)(c), (float)((c) - (double)(float)(c)))
+
 // multiply by SIGN*i
 template <class P, int SIGN>
 __device__ __forceinline__ typename P::C msi(typename P::C a) {
@@ -217,6 +231,9 @@ struct FastArgs {
   int mode;           // 0 c2c, 1 r2c, 2 c2r, 3 REDFT10, 4 REDFT01
   int Zi, Ni, Zo, No;
   int plain;
+  // adjoint weights: 1 = c2r loads halve the interior half-spectrum bins
+  // (0 < k < N/2), 2 = r2c stores double them
+  int wmode;
   const void* tw2;
 };
 
@@ -322,17 +339,17 @@ __device__ __forceinline__ typename P::C load_elem(const FastArgs& a, long long 
     return P::mul(z, P::twc(__ldg((const typename P::S*)a.tw2 + e), 1));
   }
   bool mirror = false;
-  int q;
+  int q, k = e;
   if (a.mode == 2) {
     mirror = 2 * e > N;
-    q = (mirror ? N - e : e) - a.Zi;
-  } else {
-    q = e - a.Zi;
+    k = mirror ? N - e : e;
   }
+  q = k - a.Zi;
   if (q < 0 || q >= a.Ni) return czero<P>();
   C v = a.mode == 1 ? rload<P, CG>(a.src, off + (long long)q * a.sIa)
                     : gload<P, CG>((const typename P::G*)a.src + off + (long long)q * a.sIa, a.in_df);
   if (a.conj_in) v = P::conj(v);
+  if (a.wmode == 1 && k != 0 && 2 * k != N) v = P::scal(v, PG_KC(P, 0.5));
   return mirror ? P::conj(v) : v;
 }
 
@@ -349,6 +366,7 @@ __device__ __forceinline__ void store_elem(const FastArgs& a, long long off, int
   }
   const int k = e - a.Zo;
   if (k < 0 || k >= a.No) return;
+  if (a.wmode == 2 && e != 0 && 2 * e != N) v = P::add(v, v);
   if (a.conj_out) v = P::conj(v);
   if (a.mode >= 2)
     rstore<P>(a.dst, off + (long long)k * a.sOa, v);
@@ -366,7 +384,9 @@ __device__ __forceinline__ void store_elem(const FastArgs& a, long long off, int
 // the body of the stand-alone kernel k_fast, and a task of the batched
 // persistent kernel.  `blk` is the tile index, `sm_raw` the block's dynamic
 // shared memory (fast_smem_bytes).
-template <class P, int SIGN, int N, int L, bool ROW_IN, bool ROW_OUT, bool CG = false, bool DCT = false>
+// IO: 0 plain c2c lines (the hot kernels carry no other load/store code),
+// 1 r2c / c2r / windows / adjoint weights (load_elem, store_elem), 2 the DCTs
+template <class P, int SIGN, int N, int L, bool ROW_IN, bool ROW_OUT, bool CG = false, int IO = 0>
 __device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsigned char* sm_raw) {
   typedef typename P::C C;
   typedef typename P::S S;
@@ -403,7 +423,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsi
   S* line = buf + l * LSP;
 
   C v[8];
-  if (a.plain) {
+  if constexpr (IO == 0) {
     const G* src = (const G*)a.src + offI[l] + (long long)t * a.sIa;
     const long long st = (long long)TPL * a.sIa;
 #pragma unroll
@@ -413,7 +433,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsi
     }
   } else {
 #pragma unroll
-    for (int r = 0; r < 8; r++) v[r] = load_elem<P, CG, DCT>(a, offI[l], t + r * TPL, N);
+    for (int r = 0; r < 8; r++) v[r] = load_elem<P, CG, IO == 2>(a, offI[l], t + r * TPL, N);
   }
   bf8<P, SIGN>(v);  // stage 0 (Ns = 1, no twiddles)
   int Ns = 1;
@@ -441,14 +461,14 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsi
     // v holds the last stage (Ns = N/8, k = t): outputs y[t + r*TPL]
     if (ROW_IN == ROW_OUT) {
       if (live) {
-        if (a.plain) {
+        if constexpr (IO == 0) {
           G* dst = (G*)a.dst + offO[l] + (long long)t * a.sOa;
           const long long st = (long long)TPL * a.sOa;
 #pragma unroll
           for (int r = 0; r < 8; r++) gstore<P>(dst + r * st, a.conj_out ? P::conj(v[r]) : v[r], a.out_df);
         } else {
 #pragma unroll
-          for (int r = 0; r < 8; r++) store_elem<P, DCT>(a, offO[l], t + r * TPL, v[r], N);
+          for (int r = 0; r < 8; r++) store_elem<P, IO == 2>(a, offO[l], t + r * TPL, v[r], N);
         }
       }
       return;
@@ -488,7 +508,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsi
     }
     if (ROW_IN == ROW_OUT) {
       if (live) {
-        if (a.plain) {
+        if constexpr (IO == 0) {
           G* dst = (G*)a.dst + offO[l];
 #pragma unroll
           for (int b = 0; b < NB; b++)
@@ -501,7 +521,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsi
 #pragma unroll
           for (int b = 0; b < NB; b++)
 #pragma unroll
-            for (int r = 0; r < Q; r++) store_elem<P, DCT>(a, offO[l], t + b * TPL + r * NQ, w[b * Q + r], N);
+            for (int r = 0; r < Q; r++) store_elem<P, IO == 2>(a, offO[l], t + b * TPL + r * NQ, w[b * Q + r], N);
         }
       }
       return;
@@ -524,21 +544,21 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsi
       for (int r = 0; r < 8; r++) {
         const int k = t2 + r * TPL;
         C o = P::lds(line2[pad<P>(k)]);
-        if (a.plain) {
+        if constexpr (IO == 0) {
           if (a.conj_out) o = P::conj(o);
           gstore<P>(d2 + (long long)k * a.sOa, o, a.out_df);
         } else {
-          store_elem<P, DCT>(a, offO[l2], k, o, N);
+          store_elem<P, IO == 2>(a, offO[l2], k, o, N);
         }
       }
     }
   }
 }
 
-template <class P, int SIGN, int N, int L, bool ROW_IN, bool ROW_OUT, bool DCT = false>
+template <class P, int SIGN, int N, int L, bool ROW_IN, bool ROW_OUT, int IO = 0>
 __global__ void __launch_bounds__(L*(N / 8)) k_fast(const FastArgs a) {
   extern __shared__ __align__(16) unsigned char sm_raw[];
-  fast_tile<P, SIGN, N, L, ROW_IN, ROW_OUT, false, DCT>(a, blockIdx.x, sm_raw);
+  fast_tile<P, SIGN, N, L, ROW_IN, ROW_OUT, false, IO>(a, blockIdx.x, sm_raw);
 }
 
 template <class P, int N, int L>
@@ -546,7 +566,7 @@ constexpr size_t fast_smem_bytes() {
   return 16 * L + (size_t)L * (sizeof(typename P::S) == 8 ? N + 16 : N + N / 8 + 4) * sizeof(typename P::S);
 }
 
-template <class P, int SIGN, int N, int L, bool DCT = false>
+template <class P, int SIGN, int N, int L, int IO = 0>
 int launch4(const FastArgs& a, bool row_in, bool row_out, cudaStream_t s) {
   constexpr int T = L * (N / 8);
   const size_t smem = fast_smem_bytes<P, N, L>();
@@ -558,12 +578,12 @@ int launch4(const FastArgs& a, bool row_in, bool row_out, cudaStream_t s) {
   do {                                                                                                    \
     static bool attr_done = false;                                                                        \
     if (!attr_done) {                                                                                     \
-      e = cudaFuncSetAttribute(k_fast<P, SIGN, N, L, RI, RO, DCT>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+      e = cudaFuncSetAttribute(k_fast<P, SIGN, N, L, RI, RO, IO>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                                (int)smem);                                                                \
       if (e != cudaSuccess) return (int)e;                                                                \
       attr_done = true;                                                                                   \
     }                                                                                                     \
-    k_fast<P, SIGN, N, L, RI, RO, DCT><<<(unsigned)grid, T, smem, s>>>(a);                                \
+    k_fast<P, SIGN, N, L, RI, RO, IO><<<(unsigned)grid, T, smem, s>>>(a);                                \
   } while (0)
   if (row_in && row_out)
     PG_FAST_LAUNCH(true, true);
@@ -587,6 +607,10 @@ template <class P, int SIGN>
 int launch_small(int N, const FastArgs& a, bool row_in, bool row_out, cudaStream_t s);
 template <class P, int SIGN>
 int launch_large(int N, const FastArgs& a, bool row_in, bool row_out, cudaStream_t s);
+// r2c / c2r / windowed / weighted passes of 16..4096 points, default tile
+// heights (fft_fast_gio_<arith>_<dir>.cu)
+template <class P, int SIGN>
+int launch_gio(int N, const FastArgs& a, bool row_in, bool row_out, cudaStream_t s);
 // REDFT10 (SIGN -1) / REDFT01 (SIGN +1) passes of 16..512 points with the same
 // orientation on both sides, default tile heights (fft_fast_dct_<arith>_<dir>.cu)
 template <class P, int SIGN>

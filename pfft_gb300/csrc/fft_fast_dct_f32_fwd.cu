@@ -11,13 +11,13 @@ template <class P, int SIGN>
 int launch_dct(int N, const FastArgs& a, bool row_in, bool row_out, cudaStream_t s) {
   if (row_in != row_out) return -1;
   switch (N) {
-    case 16: return launch4<P, SIGN, 16, 128, true>(a, row_in, row_out, s);
-    case 32: return launch4<P, SIGN, 32, 64, true>(a, row_in, row_out, s);
-    case 64: return launch4<P, SIGN, 64, 32, true>(a, row_in, row_out, s);
-    case 128: return launch4<P, SIGN, 128, 16, true>(a, row_in, row_out, s);
-    case 256: return launch4<P, SIGN, 256, 8, true>(a, row_in, row_out, s);
-    case 512: return row_in ? launch4<P, SIGN, 512, 4, true>(a, row_in, row_out, s)
-                            : launch4<P, SIGN, 512, 8, true>(a, row_in, row_out, s);
+    case 16: return launch4<P, SIGN, 16, 128, 2>(a, row_in, row_out, s);
+    case 32: return launch4<P, SIGN, 32, 64, 2>(a, row_in, row_out, s);
+    case 64: return launch4<P, SIGN, 64, 32, 2>(a, row_in, row_out, s);
+    case 128: return launch4<P, SIGN, 128, 16, 2>(a, row_in, row_out, s);
+    case 256: return launch4<P, SIGN, 256, 8, 2>(a, row_in, row_out, s);
+    case 512: return row_in ? launch4<P, SIGN, 512, 4, 2>(a, row_in, row_out, s)
+                            : launch4<P, SIGN, 512, 8, 2>(a, row_in, row_out, s);
   }
   return -1;
 }

@@ -40,18 +40,7 @@ struct MixedSched {
   }
 };
 
-template <class P>
-struct Kc;
-template <>
-struct Kc<F32> {
-  static __device__ __forceinline__ float k(float h, float) { return h; }
-};
-template <>
-struct Kc<FDD> {
-  static __device__ __forceinline__ DD k(float h, float l) { return {h, l}; }
-};
-// a double constant split at compile time into float hi + lo
-#define PG_KC(P, c) Kc<P>::k((float)(c), (float)((c) - (double)(float)(c)))
+
 
 template <class P, int SIGN>
 __device__ __forceinline__ void bf2(typename P::C* v) {
@@ -210,8 +199,9 @@ __device__ __forceinline__ void mixed_tile(const FastArgs& a, long long blk, uns
   const S* tw = (const S*)a.tw;
   S* line = buf + l * LSP;
 
+  // plain c2c lines only (fast_args sends no other mode here)
   C v[E];
-  if (a.plain) {
+  {
     const G* src = (const G*)a.src + offI[l];
 #pragma unroll
     for (int i = 0; i < E / R0; i++)
@@ -221,11 +211,6 @@ __device__ __forceinline__ void mixed_tile(const FastArgs& a, long long blk, uns
         C x = gload<P, CG>(src + e * a.sIa, a.in_df);
         v[i * R0 + r] = a.conj_in ? P::conj(x) : x;
       }
-  } else {
-#pragma unroll
-    for (int i = 0; i < E / R0; i++)
-#pragma unroll
-      for (int r = 0; r < R0; r++) v[i * R0 + r] = load_elem<P, CG>(a, offI[l], t + i * TPL + r * (N / R0), N);
   }
   mixed_stages<P, SIGN, N, E, 0>(v, t, tw, line);
   // last stage: output r of butterfly i is element t + i * TPL + r * N/RL
@@ -238,10 +223,7 @@ __device__ __forceinline__ void mixed_tile(const FastArgs& a, long long blk, uns
         for (int r = 0; r < RL; r++) {
           const int e = t + i * TPL + r * (N / RL);
           C o = v[i * RL + r];
-          if (a.plain)
-            gstore<P>(dst + (long long)e * a.sOa, a.conj_out ? P::conj(o) : o, a.out_df);
-          else
-            store_elem<P>(a, offO[l], e, o, N);
+          gstore<P>(dst + (long long)e * a.sOa, a.conj_out ? P::conj(o) : o, a.out_df);
         }
     }
     return;
@@ -262,10 +244,7 @@ __device__ __forceinline__ void mixed_tile(const FastArgs& a, long long blk, uns
     for (int q = 0; q < E; q++) {
       const int k = t2 + q * TPL;
       C o = P::lds(line2[pad<P>(k)]);
-      if (a.plain)
-        gstore<P>(d2 + (long long)k * a.sOa, a.conj_out ? P::conj(o) : o, a.out_df);
-      else
-        store_elem<P>(a, offO[l2], k, o, N);
+      gstore<P>(d2 + (long long)k * a.sOa, a.conj_out ? P::conj(o) : o, a.out_df);
     }
   }
 }

@@ -76,10 +76,12 @@ std::vector<Choice> candidates(const PassParams& p, int arith) {
     v.push_back(c);
     // the other tile heights instantiated for this length (fft_fast_*_[sl].cu)
     std::vector<int> alt;
-    if (p.N == 512) alt = {4, 8, 16};
-    if (p.N == 1024) alt = {2, 4, 8};
-    if (p.N == 2048) alt = {2, 4};
-    if (p.N == 4096) alt = {1, 2};
+    const bool plain = p.mode == MODE_C2C && p.Zi == 0 && p.Ni == p.N && p.Zo == 0 && p.No == p.N && !p.wmode;
+    // (the r2c / c2r / windowed instantiations have their default heights only)
+    if (plain && p.N == 512) alt = {4, 8, 16};
+    if (plain && p.N == 1024) alt = {2, 4, 8};
+    if (plain && p.N == 2048) alt = {2, 4};
+    if (plain && p.N == 4096) alt = {1, 2};
     for (int Lf : alt) {
       c.fastL = Lf;
       v.push_back(c);
