@@ -120,6 +120,21 @@ int pfft_gb300_wisdom_entries(void);
 void pfft_gb300_set_kernel_path(int path);
 int pfft_gb300_get_kernel_path(void);
 
+/* Staged variant of the radix-8 kernel for plain c2c passes: persistent CTAs
+ * whose next tile is copied global -> shared memory by the copy engine
+ * (bulk / tensor-map copies on an mbarrier) while the current tile is
+ * transformed.  1 (default): per pass, as the autotuner or wisdom chose, else
+ * on for float column passes; 2: wherever the pass layout allows; 0: off
+ * (also PFFT_GB300_STAGED=0/1/2).  staged_launches counts its launches in
+ * this process.  staged_status waits for the device, returns 1 if a staged
+ * load wait expired since the last call (the results of that execute are
+ * wrong), 0 if not, or a negative cudaError_t value, and clears the flag.
+ * No counterpart in the reference's API. */
+void pfft_gb300_set_staged(int mode);
+int pfft_gb300_get_staged(void);
+long long pfft_gb300_staged_launches(void);
+int pfft_gb300_staged_status(void);
+
 /* Ghost-cell exchange that allocates nothing.  No counterpart in the
  * reference PFFT.  For callers that cannot allocate device memory when they
  * need the halo (solver loops that pre-size every buffer, memory-pool budgets,

@@ -197,6 +197,10 @@ def _declare(L):
     L.pfft_gb300_set_kernel_path.argtypes = [ctypes.c_int]
     L.pfft_gb300_get_kernel_path.restype = ctypes.c_int
     L.pfft_gb300_get_double_arith.restype = ctypes.c_int
+    L.pfft_gb300_set_staged.argtypes = [ctypes.c_int]
+    L.pfft_gb300_get_staged.restype = ctypes.c_int
+    L.pfft_gb300_staged_launches.restype = ctypes.c_longlong
+    L.pfft_gb300_staged_status.restype = ctypes.c_int
 
 
 def export_wisdom():

@@ -411,6 +411,18 @@ const char* pfft_gb300_last_error_string(void) { return last_error_string(); }
 void pfft_gb300_clear_error(void) { clear_error(); }
 void pfft_gb300_set_kernel_path(int path) { set_kernel_path(path ? 1 : 0); }
 int pfft_gb300_get_kernel_path(void) { return kernel_path(); }
+void pfft_gb300_set_staged(int mode) { set_staged_mode(mode); }
+int pfft_gb300_get_staged(void) { return staged_mode(); }
+long long pfft_gb300_staged_launches(void) { return staged_launches(); }
+int pfft_gb300_staged_status(void) {
+  int* w = staged_err_word_if_any();
+  if (!w) return 0;
+  int h = 0;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(&h, w, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemset(w, 0, sizeof(int));
+  return e == cudaSuccess ? (h ? 1 : 0) : -(int)e;
+}
 int pfft_gb300_set_double_arith(int mode) {
   if (mode != DARITH_DF && mode != DARITH_NATIVE && mode != DARITH_AUTO) return -1;
   set_double_arith(mode);

@@ -1,11 +1,135 @@
 // Dispatcher of the register-resident radix-8 pass kernel (fft_fast.cuh).
+#include <atomic>
+#include <mutex>
+#include <string.h>
+#include <cudaTypedefs.h>
 #include "fft_fast.cuh"
 #include "fft_mixed.cuh"
 #include "core.h"
 
 namespace pg {
 
+static int g_staged = -1;  // 0 off, 1 per-pass choice, 2 wherever the layout allows
+static std::atomic<long long> g_staged_launches{0};
+int staged_mode() {
+  if (g_staged < 0) {
+    const char* e = getenv("PFFT_GB300_STAGED");
+    g_staged = (e && strcmp(e, "0") == 0) ? 0 : (e && strcmp(e, "2") == 0) ? 2 : 1;
+  }
+  return g_staged;
+}
+void set_staged_mode(int v) { g_staged = (v >= 0 && v <= 2) ? v : 1; }
+long long staged_launches() { return g_staged_launches.load(); }
+
 namespace fast {
+
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)f;
+  });
+  return fn;
+}
+
+int sm_count() {
+  static int n[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return 1;
+  if (!n[dev]) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    n[dev] = v > 0 ? v : 1;
+  }
+  return n[dev];
+}
+
+// one error word per device, zeroed when allocated
+static int* g_err[64] = {nullptr};
+static std::mutex g_err_mu;
+int* staged_err_word() {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  if (!g_err[dev]) {
+    int* p = nullptr;
+    if (cudaMalloc(&p, sizeof(int)) != cudaSuccess) return nullptr;
+    if (cudaMemset(p, 0, sizeof(int)) != cudaSuccess) {
+      cudaFree(p);
+      return nullptr;
+    }
+    g_err[dev] = p;
+  }
+  return g_err[dev];
+}
+
+}  // namespace fast
+
+int* staged_err_word_if_any() {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lk(fast::g_err_mu);
+  return fast::g_err[dev];
+}
+
+namespace fast {
+bool staged_setup(const FastArgs& a, int N, int L, int esz, bool row_in, CUtensorMap* tm) {
+  if (!staged_mode() || a.nlines <= 0 || ((uintptr_t)a.src & 15)) return false;
+  // default: float column passes (measured: the float-float kernels are
+  // bound by instruction issue and lose a resident CTA per SM to the staging
+  // area; row passes load whole lines with full coalescing already)
+  if (staged_mode() == 1 && (a.staged == 2 || (a.staged == 0 && (esz != 8 || row_in)))) return false;
+  if (row_in) {
+    // every line's copy starts on a 16-byte boundary and is N * esz bytes
+    if (a.sIa != 1 || (N * esz) % 16) return false;
+    for (int b = 0; b < a.nb; b++)
+      if ((a.bsI[b] * esz) % 16) return false;
+    memset(tm, 0, sizeof *tm);
+    g_staged_launches++;
+    return true;
+  }
+  // column tiles: L adjacent lines along batch dimension 0, never straddling it
+  if (a.nb < 1 || a.nb > 4 || a.bsI[0] != 1 || a.bext[0] % L || (L * esz) % 16 || L * esz / 4 > 256) return false;
+  PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
+  if (!enc) return false;
+  const int words = esz / 4;
+  cuuint64_t dims[5], strides[4];
+  cuuint32_t box[5], estr[5] = {1, 1, 1, 1, 1};
+  dims[0] = (cuuint64_t)a.bext[0] * words;
+  dims[1] = (cuuint64_t)N;
+  strides[0] = (cuuint64_t)a.sIa * esz;
+  box[0] = (cuuint32_t)(L * words);
+  box[1] = (cuuint32_t)(N < 256 ? N : 256);
+  for (int d = 2; d < 5; d++) {
+    const int b = d - 1;
+    if (b < a.nb) {
+      dims[d] = (cuuint64_t)a.bext[b];
+      strides[d - 1] = (cuuint64_t)a.bsI[b] * esz;
+    } else {
+      dims[d] = 1;
+      strides[d - 1] = strides[d - 2];
+    }
+    box[d] = 1;
+  }
+  for (int d = 0; d < 4; d++)
+    if (strides[d] % 16 || strides[d] >= (1ull << 40)) return false;
+  for (int d = 0; d < 5; d++)
+    if (dims[d] > (1ull << 32)) return false;
+  CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_UINT32, 5, (void*)a.src, dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return false;
+  g_staged_launches++;
+  return true;
+}
+
 bool fast_args(const PassParams& p, int arith, FastArgs* a, bool* row_in, bool* row_out) {
   const bool dct = p.mode == MODE_RE10 || p.mode == MODE_RE01;
   if ((p.mode != MODE_C2C && p.mode != MODE_R2C && p.mode != MODE_C2R && !dct) || p.nst == 0) return false;
@@ -77,6 +201,7 @@ int launch_fast_pass(const PassParams& p, int arith, cudaStream_t stream) {
   const int N = p.N;
   const bool big = N >= 1024;
   a.fastL = p.fastL;
+  a.staged = p.staged;
   // the FFT direction: the pass's, except for the DCTs (10 forward, 01 inverse)
   const int sign = a.mode == 3 ? -1 : (a.mode == 4 ? 1 : p.sign);
   if (a.mode >= 3)

@@ -17,8 +17,10 @@
 //     once per butterfly output.
 // A length N = 8^a * q (q = 1, 2, 4) runs a radix-8 stages and one radix-q stage.
 #pragma once
+#include <algorithm>
 #include "arith.cuh"
 #include "pass.h"
+#include "tma.cuh"
 
 namespace pg {
 
@@ -235,6 +237,7 @@ struct FastArgs {
   // (0 < k < N/2), 2 = r2c stores double them
   int wmode;
   const void* tw2;
+  int staged;  // host only: PassParams::staged
 };
 
 // global element access: native format, or float-float pairs for the
@@ -384,6 +387,9 @@ __device__ __forceinline__ void store_elem(const FastArgs& a, long long off, int
 // the body of the stand-alone kernel k_fast, and a task of the batched
 // persistent kernel.  `blk` is the tile index, `sm_raw` the block's dynamic
 // shared memory (fast_smem_bytes).
+template <class P, int SIGN, int N, int L, bool ROW_IN, bool ROW_OUT, int IO>
+__device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[8], long long g0, const long long* offO,
+                                          typename P::S* buf);
 // IO: 0 plain c2c lines (the hot kernels carry no other load/store code),
 // 1 r2c / c2r / windows / adjoint weights (load_elem, store_elem), 2 the DCTs
 template <class P, int SIGN, int N, int L, bool ROW_IN, bool ROW_OUT, bool CG = false, int IO = 0>
@@ -392,9 +398,6 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsi
   typedef typename P::S S;
   typedef typename P::G G;
   constexpr int TPL = N / 8;  // threads per line
-  constexpr int NS8 = n8_of(N);
-  constexpr int Q = N / pow8(NS8);  // last radix: 1, 2 or 4
-  constexpr int LSP = lsp_of<P, N, L, ROW_IN>();
   long long* offI = (long long*)sm_raw;
   long long* offO = offI + L;
   S* buf = (S*)(sm_raw + 16 * L);
@@ -418,9 +421,6 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsi
   __syncthreads();
   const int l = ROW_IN ? tid / TPL : tid % L;
   const int t = ROW_IN ? tid % TPL : tid / L;
-  const bool live = (g0 + l) < a.nlines;
-  const S* tw = (const S*)a.tw;
-  S* line = buf + l * LSP;
 
   C v[8];
   if constexpr (IO == 0) {
@@ -435,6 +435,28 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsi
 #pragma unroll
     for (int r = 0; r < 8; r++) v[r] = load_elem<P, CG, IO == 2>(a, offI[l], t + r * TPL, N);
   }
+  fast_body<P, SIGN, N, L, ROW_IN, ROW_OUT, IO>(a, v, g0, offO, buf);
+}
+
+// Stages and store of one tile after the load: v holds elements t + r*TPL of
+// line l (the input thread mapping); offO the output offsets of the tile's
+// lines; buf the exchange area (L lines of lsp_of elements).
+template <class P, int SIGN, int N, int L, bool ROW_IN, bool ROW_OUT, int IO>
+__device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[8], long long g0, const long long* offO,
+                                          typename P::S* buf) {
+  typedef typename P::C C;
+  typedef typename P::S S;
+  typedef typename P::G G;
+  constexpr int TPL = N / 8;  // threads per line
+  constexpr int NS8 = n8_of(N);
+  constexpr int Q = N / pow8(NS8);  // last radix: 1, 2 or 4
+  constexpr int LSP = lsp_of<P, N, L, ROW_IN>();
+  const int tid = threadIdx.x;
+  const int l = ROW_IN ? tid / TPL : tid % L;
+  const int t = ROW_IN ? tid % TPL : tid / L;
+  const bool live = (g0 + l) < a.nlines;
+  const S* tw = (const S*)a.tw;
+  S* line = buf + l * LSP;
   bf8<P, SIGN>(v);  // stage 0 (Ns = 1, no twiddles)
   int Ns = 1;
   // radix-8 stages 1 .. NS8-1 through shared memory
@@ -566,10 +588,171 @@ constexpr size_t fast_smem_bytes() {
   return 16 * L + (size_t)L * (sizeof(typename P::S) == 8 ? N + 16 : N + N / 8 + 4) * sizeof(typename P::S);
 }
 
+// ---- staged persistent variant (plain c2c passes) ---------------------------
+// Each CTA walks the tiles blockIdx.x, blockIdx.x + gridDim.x, ...  The input
+// of its next tile is copied global -> shared memory by the copy engine while
+// the current tile is transformed: row tiles as one cp.async.bulk per line,
+// column tiles (L adjacent lines) as tensor-map boxes of L lines x up to 256
+// elements.  The copies complete on an mbarrier; the threads read their eight
+// elements from the staging area, the area is released by a CTA barrier and
+// the next tile's copies are issued before the stages run.  So the global
+// loads' latency is off the critical path and no registers hold a second
+// tile.  Shared memory: up to 128 bytes of alignment, staging (L*N elements in
+// the global format), the mbarrier (16 bytes), two sets of output offsets,
+// the exchange area.
+template <class P, int N, int L>
+constexpr size_t staged_smem_bytes() {
+  return 128 + (size_t)L * N * sizeof(typename P::G) + 16 + fast_smem_bytes<P, N, L>();
+}
+// a staged-load wait gives up after this many nanoseconds (error word set)
+constexpr unsigned long long STAGED_WAIT_NS = 2000000000ull;
+
+template <class P, int SIGN, int N, int L, bool ROW_IN, bool ROW_OUT>
+__global__ void __launch_bounds__(L*(N / 8))
+    k_fast_staged(const __grid_constant__ FastArgs a, const __grid_constant__ CUtensorMap tm, int* err) {
+  typedef typename P::C C;
+  typedef typename P::G G;
+  typedef typename P::S S;
+  constexpr int TPL = N / 8;
+  constexpr int ESZ = (int)sizeof(G);
+  constexpr uint32_t LINE_BYTES = (uint32_t)N * ESZ;
+  constexpr int BOX = N < 256 ? N : 256;  // elements per tensor box (column tiles)
+  extern __shared__ __align__(16) unsigned char sm_dyn[];
+  // staging area on a 128-byte boundary (tensor-map copies)
+  unsigned char* sm_raw = sm_dyn + ((128u - (tma::smem_addr(sm_dyn) & 127u)) & 127u);
+  const G* stage = (const G*)sm_raw;
+  const uint32_t st_addr = tma::smem_addr(sm_raw);
+  const uint32_t mb = st_addr + L * LINE_BYTES;
+  long long* offO2 = (long long*)(sm_raw + L * LINE_BYTES + 16);
+  S* buf = (S*)(sm_raw + L * LINE_BYTES + 16 + 16 * L);
+  const int tid = threadIdx.x;
+  const long long ntiles = (a.nlines + L - 1) / L;
+  if (tid == 0) {
+    tma::mbar_init(mb, 1);
+    tma::mbar_init_fence();
+    if (!ROW_IN) tma::prefetch_tensormap(&tm);
+  }
+  __syncthreads();
+  // copies of tile tl: row tiles one line per lane 0..L-1, column tiles by thread 0
+  auto issue = [&](long long tl) {
+    const long long g0 = tl * L;
+    if constexpr (ROW_IN) {
+      if (tid < L) {
+        const long long nv = min((long long)L, a.nlines - g0);
+        if (tid == 0) tma::mbar_arrive_tx(mb, (uint32_t)nv * LINE_BYTES);
+        if (tid < nv) {
+          long long g = g0 + tid, oi = 0;
+          for (int b = 0; b < a.nb; b++) {
+            const long long e = a.bext[b];
+            oi += (g % e) * a.bsI[b];
+            g /= e;
+          }
+          tma::bulk_load(st_addr + tid * LINE_BYTES, (const G*)a.src + oi, LINE_BYTES, mb);
+        }
+      }
+    } else {
+      if (tid == 0) {
+        // the tile's lines are adjacent along batch dimension 0 (extent a
+        // multiple of L); tensor dimensions: 4-byte words of dimension 0,
+        // elements, batch dimensions 1..3
+        long long g = g0;
+        const int c0 = (int)(g % a.bext[0]) * (ESZ / 4);
+        g /= a.bext[0];
+        int c[3] = {0, 0, 0};
+        for (int b = 1; b < a.nb; b++) {
+          c[b - 1] = (int)(g % a.bext[b]);
+          g /= a.bext[b];
+        }
+        tma::mbar_arrive_tx(mb, L * LINE_BYTES);
+#pragma unroll
+        for (int e0 = 0; e0 < N; e0 += BOX) tma::tensor_load5(st_addr + e0 * L * ESZ, &tm, c0, e0, c[0], c[1], c[2], mb);
+      }
+    }
+  };
+  long long tile = blockIdx.x;
+  if (tile < ntiles) issue(tile);
+  uint32_t parity = 0;
+  int sel = 0;
+  for (; tile < ntiles; tile += gridDim.x, parity ^= 1, sel ^= 1) {
+    const long long g0 = tile * L;
+    long long* offO = offO2 + sel * L;
+    if (tid < L) {
+      long long g = g0 + tid;
+      if (g >= a.nlines) g = a.nlines - 1;  // tail tile: never stored
+      long long oo = 0;
+      for (int b = 0; b < a.nb; b++) {
+        const long long e = a.bext[b];
+        oo += (g % e) * a.bsO[b];
+        g /= e;
+      }
+      offO[tid] = oo;
+    }
+    const bool ok = tma::mbar_wait(mb, parity, STAGED_WAIT_NS);
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) {
+        atomicExch(err, 1);
+        tma::mbar_wait(mb, parity, STAGED_WAIT_NS);  // the copies of this tile, bounded
+      }
+      return;
+    }
+    const int l = ROW_IN ? tid / TPL : tid % L;
+    const int t = ROW_IN ? tid % TPL : tid / L;
+    C v[8];
+#pragma unroll
+    for (int r = 0; r < 8; r++) {
+      const int e = t + r * TPL;
+      v[r] = gload<P, false>(ROW_IN ? stage + l * N + e : stage + e * L + l, a.in_df);
+      if (a.conj_in) v[r] = P::conj(v[r]);
+    }
+    __syncthreads();  // staging area free; offO visible; the previous tile is done
+    if (tile + gridDim.x < ntiles) issue(tile + gridDim.x);
+    fast_body<P, SIGN, N, L, ROW_IN, ROW_OUT, 0>(a, v, g0, offO, buf);
+  }
+}
+
+// Host side of the staged variant (fft_fast.cu): false when the pass cannot
+// be staged with L lines per tile (disabled, alignment, a column tile that
+// would straddle batch dimension 0, more than 4 batch dimensions); fills the
+// tensor map of column tiles.
+bool staged_setup(const FastArgs& a, int N, int L, int esz, bool row_in, CUtensorMap* tm);
+int* staged_err_word();
+int sm_count();
+
+template <class P, int SIGN, int N, int L, bool RI, bool RO>
+int launch_staged(const FastArgs& a, const CUtensorMap& tm, cudaStream_t s) {
+  constexpr int T = L * (N / 8);
+  constexpr size_t smem = staged_smem_bytes<P, N, L>();
+  static int per_sm = 0;  // resident CTAs per SM, found once per instantiation
+  if (!per_sm) {
+    cudaError_t e = cudaFuncSetAttribute(k_fast_staged<P, SIGN, N, L, RI, RO>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return (int)e;
+    int nb = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_fast_staged<P, SIGN, N, L, RI, RO>, T, smem);
+    if (e != cudaSuccess) return (int)e;
+    per_sm = nb > 0 ? nb : 1;
+  }
+  int* err = staged_err_word();
+  if (!err) return (int)cudaErrorMemoryAllocation;
+  const long long ntiles = (a.nlines + L - 1) / L;
+  const long long grid = std::min(ntiles, (long long)per_sm * sm_count());
+  k_fast_staged<P, SIGN, N, L, RI, RO><<<(unsigned)grid, T, smem, s>>>(a, tm, err);
+  return (int)cudaGetLastError();
+}
+
 template <class P, int SIGN, int N, int L, int IO = 0>
 int launch4(const FastArgs& a, bool row_in, bool row_out, cudaStream_t s) {
   constexpr int T = L * (N / 8);
   const size_t smem = fast_smem_bytes<P, N, L>();
+  if constexpr (IO == 0 && staged_smem_bytes<P, N, L>() <= 227 * 1024) {
+    CUtensorMap tm;
+    if (staged_setup(a, N, L, (int)sizeof(typename P::G), row_in, &tm)) {
+      if (row_in && row_out) return launch_staged<P, SIGN, N, L, true, true>(a, tm, s);
+      if (!row_in && !row_out) return launch_staged<P, SIGN, N, L, false, false>(a, tm, s);
+      if (row_in) return launch_staged<P, SIGN, N, L, true, false>(a, tm, s);
+      return launch_staged<P, SIGN, N, L, false, true>(a, tm, s);
+    }
+  }
   long long grid = (a.nlines + L - 1) / L;
   if (grid > 2147483647LL) return (int)cudaErrorInvalidConfiguration;
   cudaError_t e = cudaSuccess;

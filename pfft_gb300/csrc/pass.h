@@ -77,6 +77,8 @@ struct PassParams {
   int smem_bytes;
   int kpath;    // 0: register-resident radix-8 kernel where it applies, 1: general kernel
   int fastL;    // radix-8 kernel lines per CTA (0: default for the length)
+  int staged;   // staged variant of the radix-8 kernel (plain c2c passes): 0 default
+                // (float column passes), 1 on where the layout allows, 2 off
 };
 
 // Launch one pass on `stream`.  Returns a cudaError_t value.
@@ -86,6 +88,13 @@ int kernel_path();
 // true when launch_pass runs this pass on the register-resident radix-8 kernel
 bool fast_pass_eligible(const PassParams& p, int arith);
 void set_kernel_path(int v);
+// staged persistent variant of the radix-8 kernel for plain c2c passes:
+// 1 per pass as PassParams::staged says (default), 2 wherever the layout
+// allows, 0 off (PFFT_GB300_STAGED=0/1/2)
+int staged_mode();
+void set_staged_mode(int v);
+long long staged_launches();  // staged launches so far in this process
+int* staged_err_word_if_any();  // the current device's error word, or null if none was made
 
 // Shared-memory element size of a policy.
 inline int arith_sm_bytes(int arith) { return arith == ARITH_F32 ? 8 : 16; }

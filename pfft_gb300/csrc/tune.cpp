@@ -11,9 +11,13 @@
 // the choice is recorded as wisdom under a key that describes the pass
 // completely (arithmetic, mode, lengths, strides, batch shape, flags), so any
 // later plan with the same pass - created with any flags - uses it without
-// timing (a tuning planner also skips passes already in wisdom).  Wisdom is exported and imported as text:
-//   pfft_gb300-wisdom 1
-//   <key> <kpath> <fastL> <pref> <L>
+// timing (a tuning planner also skips passes already in wisdom).  Plain c2c
+// passes on the radix-8 kernel are also timed with and without its staged
+// variant.  Wisdom is exported and imported as text:
+//   pfft_gb300-wisdom 2
+//   <key> <kpath> <fastL> <pref> <L> <staged>
+// (files with the header "pfft_gb300-wisdom 1" and no staged field are read
+// with staged = 0, the default).
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -35,6 +39,7 @@ struct Choice {
   int fastL = 0;
   int pref = 0;   // radix order of the general kernel
   int L = 0;      // lines per CTA of the general kernel
+  int staged = 0; // staged variant of the radix-8 kernel: 0 default, 1 on, 2 off
 };
 
 std::mutex g_mu;
@@ -43,7 +48,8 @@ std::map<std::string, Choice>& store() {
   return m;
 }
 
-const char* kHeader = "pfft_gb300-wisdom 1";
+const char* kHeader = "pfft_gb300-wisdom 2";
+const char* kHeader1 = "pfft_gb300-wisdom 1";  // without the staged field (read as 0)
 
 std::string key_of(const PassParams& p, int arith) {
   std::ostringstream k;
@@ -59,6 +65,7 @@ bool apply_choice(PassParams* p, int arith, const Choice& c) {
   PassParams q = *p;
   q.kpath = c.kpath;
   q.fastL = c.fastL;
+  q.staged = c.staged;
   if (c.kpath == 1 || !fast_pass_eligible(q, arith)) {
     if (!refit_pass(&q, arith, c.pref, c.L)) return false;
   }
@@ -85,6 +92,16 @@ std::vector<Choice> candidates(const PassParams& p, int arith) {
     for (int Lf : alt) {
       c.fastL = Lf;
       v.push_back(c);
+    }
+    // plain c2c passes: each tile height with and without the staged variant
+    if (plain && staged_mode() == 1) {
+      const size_t n = v.size();
+      for (size_t i = 0; i < n; i++) {
+        v[i].staged = 2;
+        Choice d = v[i];
+        d.staged = 1;
+        v.push_back(d);
+      }
     }
   }
   const int L0 = p.L;
@@ -232,7 +249,7 @@ char* pfft_gb300_export_wisdom_to_string(void) {
     std::lock_guard<std::mutex> lk(g_mu);
     for (const auto& kv : store())
       o << kv.first << " " << kv.second.kpath << " " << kv.second.fastL << " " << kv.second.pref << " "
-        << kv.second.L << "\n";
+        << kv.second.L << " " << kv.second.staged << "\n";
   }
   std::string s = o.str();
   char* r = (char*)malloc(s.size() + 1);
@@ -244,7 +261,8 @@ int pfft_gb300_import_wisdom_from_string(const char* text) {
   if (!text) return 0;
   std::istringstream in(text);
   std::string line;
-  if (!std::getline(in, line) || line != kHeader) return 0;
+  if (!std::getline(in, line) || (line != kHeader && line != kHeader1)) return 0;
+  const bool v2 = line == kHeader;
   std::map<std::string, Choice> add;
   while (std::getline(in, line)) {
     if (line.empty()) continue;
@@ -252,7 +270,10 @@ int pfft_gb300_import_wisdom_from_string(const char* text) {
     std::string key;
     Choice c;
     if (!(ls >> key >> c.kpath >> c.fastL >> c.pref >> c.L)) return 0;
-    if (c.kpath < 0 || c.kpath > 1 || c.pref < 0 || c.pref > 2 || c.L < 0 || c.fastL < 0) return 0;
+    if (v2 && !(ls >> c.staged)) return 0;
+    if (c.kpath < 0 || c.kpath > 1 || c.pref < 0 || c.pref > 2 || c.L < 0 || c.fastL < 0 || c.staged < 0 ||
+        c.staged > 2)
+      return 0;
     add[key] = c;
   }
   std::lock_guard<std::mutex> lk(g_mu);
