@@ -13,8 +13,11 @@
 //   * a shared-memory layout (pad, lsp_of) that keeps the stage exchanges
 //     free of bank conflicts;
 //   * for the double API, float-float arithmetic with unnormalised additions
-//     (TwoSum on the high parts, plain sums of the low parts) renormalised
-//     once per butterfly output.
+//     (TwoSum on the high parts, plain sums of the low parts); values cross
+//     the shared-memory exchanges unnormalised (an unevaluated sum hi + lo
+//     whose low part is a sum of rounding errors: its own rounding error is
+//     2^-24 |lo|, below 2^-45 of the operands' magnitude), and are
+//     renormalised only when written to global memory.
 // A length N = 8^a * q (q = 1, 2, 4) runs a radix-8 stages and one radix-q stage.
 #pragma once
 #include <algorithm>
@@ -217,7 +220,7 @@ struct FastArgs {
   long long nlines;
   int conj_in, conj_out;
   int in_df, out_df;  // double API: the array holds float-float pairs (an intermediate)
-  int fastL;          // requested lines per CTA (0: default): 512 takes 4, 8, 16; 1024 takes 2, 4, 8;
+  int fastL;          // requested lines per CTA (0: default): 512 takes 2, 4, 8, 16; 1024 takes 2, 4, 8;
                       // 2048 takes 2, 4; 4096 takes 1, 2
   // logical sequence of a line (pass_tile.cuh semantics): element e of the
   // length-N input is input element e - Zi when 0 <= e - Zi < Ni, else 0
@@ -467,7 +470,7 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
       const int k = t % Ns;
       const int base = (t - k) * 8 + k;
 #pragma unroll
-      for (int r = 0; r < 8; r++) line[pad<P>(base + r * Ns)] = P::sts(P::renorm(v[r]));
+      for (int r = 0; r < 8; r++) line[pad<P>(base + r * Ns)] = P::sts(v[r]);
     }
     __syncthreads();
     Ns *= 8;
@@ -497,7 +500,7 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
     }
     __syncthreads();
 #pragma unroll
-    for (int r = 0; r < 8; r++) line[pad<P>(t + r * TPL)] = P::sts(P::renorm(v[r]));
+    for (int r = 0; r < 8; r++) line[pad<P>(t + r * TPL)] = P::sts(v[r]);
   } else {
     // radix-Q stage (Q = 2 or 4) with Ns = N/Q: butterflies j = t + b*TPL, k = j
     if (NS8 > 1) __syncthreads();
@@ -505,7 +508,7 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
       const int k = t % Ns;
       const int base = (t - k) * 8 + k;
 #pragma unroll
-      for (int r = 0; r < 8; r++) line[pad<P>(base + r * Ns)] = P::sts(P::renorm(v[r]));
+      for (int r = 0; r < 8; r++) line[pad<P>(base + r * Ns)] = P::sts(v[r]);
     }
     __syncthreads();
     constexpr int NB = 8 / Q;
@@ -552,7 +555,7 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
 #pragma unroll
     for (int b = 0; b < NB; b++)
 #pragma unroll
-      for (int r = 0; r < Q; r++) line[pad<P>(t + b * TPL + r * NQ)] = P::sts(P::renorm(w[b * Q + r]));
+      for (int r = 0; r < Q; r++) line[pad<P>(t + b * TPL + r * NQ)] = P::sts(w[b * Q + r]);
   }
   // re-staged store with the output's thread mapping
   __syncthreads();

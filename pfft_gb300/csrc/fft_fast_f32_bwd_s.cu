@@ -16,6 +16,7 @@ int launch_small(int N, const FastArgs& a, bool row_in, bool row_out, cudaStream
     case 512: {
       const int L = a.fastL ? a.fastL : (col ? 8 : 4);
       if (L == 16) return launch4<P, SIGN, 512, 16>(a, row_in, row_out, s);
+      if (L == 2) return launch4<P, SIGN, 512, 2>(a, row_in, row_out, s);
       return L == 8 ? launch4<P, SIGN, 512, 8>(a, row_in, row_out, s) : launch4<P, SIGN, 512, 4>(a, row_in, row_out, s);
     }
   }

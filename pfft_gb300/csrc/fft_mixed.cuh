@@ -149,7 +149,7 @@ __device__ __forceinline__ void mixed_stages(typename P::C* v, int t, const type
 #pragma unroll
     for (int i = 0; i < E / St::R; i++)
 #pragma unroll
-      for (int r = 0; r < St::R; r++) line[pad<P>(St::out_pos(t, i, r))] = P::sts(P::renorm(v[i * St::R + r]));
+      for (int r = 0; r < St::R; r++) line[pad<P>(St::out_pos(t, i, r))] = P::sts(v[i * St::R + r]);
     __syncthreads();
     constexpr int R2 = MixedSched<N>::template radix<E>(s + 1);
 #pragma unroll
@@ -233,7 +233,7 @@ __device__ __forceinline__ void mixed_tile(const FastArgs& a, long long blk, uns
 #pragma unroll
   for (int i = 0; i < E / RL; i++)
 #pragma unroll
-    for (int r = 0; r < RL; r++) line[pad<P>(t + i * TPL + r * (N / RL))] = P::sts(P::renorm(v[i * RL + r]));
+    for (int r = 0; r < RL; r++) line[pad<P>(t + i * TPL + r * (N / RL))] = P::sts(v[i * RL + r]);
   __syncthreads();
   const int l2 = ROW_OUT ? tid / TPL : tid % L;
   const int t2 = ROW_OUT ? tid % TPL : tid / L;

@@ -1,7 +1,7 @@
 // Autotuner and wisdom.
 //
 // A pass can run with several equivalent configurations: the register-resident
-// radix-8 kernel (4, 8 or 16 lines per CTA at 512 points, 2, 4 or 8 at 1024,
+// radix-8 kernel (2, 4, 8 or 16 lines per CTA at 512 points, 2, 4 or 8 at 1024,
 // 2 or 4 at 2048, 1 or 2 at 4096) or
 // the general kernel with radix order 16-first / 8-first / 4-first and half,
 // the planned or twice the planned lines per CTA.  Plans created with
@@ -85,7 +85,7 @@ std::vector<Choice> candidates(const PassParams& p, int arith) {
     std::vector<int> alt;
     const bool plain = p.mode == MODE_C2C && p.Zi == 0 && p.Ni == p.N && p.Zo == 0 && p.No == p.N && !p.wmode;
     // (the r2c / c2r / windowed instantiations have their default heights only)
-    if (plain && p.N == 512) alt = {4, 8, 16};
+    if (plain && p.N == 512) alt = {2, 4, 8, 16};
     if (plain && p.N == 1024) alt = {2, 4, 8};
     if (plain && p.N == 2048) alt = {2, 4};
     if (plain && p.N == 4096) alt = {1, 2};
