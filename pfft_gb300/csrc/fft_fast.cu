@@ -130,6 +130,25 @@ bool staged_setup(const FastArgs& a, int N, int L, int esz, bool row_in, CUtenso
   return true;
 }
 
+// Twiddle tables of a pass on the radix-8 (pow2) or mixed-radix kernel: the
+// FFT's table (stage-major for radix-8, natural for mixed-radix; float-float
+// packed and of the FFT's direction: the DCTs run 10 forward, 01 inverse) and
+// the DCT's 4N-point rotation table (natural; forward for FP32).
+static bool fast_tables(const PassParams& p, int arith, bool pow2, const void** tw, const void** tw2) {
+  cudaError_t e;
+  const bool dct = p.mode == MODE_RE10 || p.mode == MODE_RE01;
+  const int fsign = p.mode == MODE_RE10 ? -1 : (p.mode == MODE_RE01 ? 1 : p.sign);
+  if (arith == ARITH_DF) {
+    *tw = twiddle_table(p.N, pow2 ? (fsign < 0 ? TW_DFP_FWD_STG : TW_DFP_BWD_STG) : (fsign < 0 ? TW_DFP_FWD : TW_DFP_BWD),
+                        &e);
+    if (dct) *tw2 = twiddle_table(p.M, fsign < 0 ? TW_DFP_FWD : TW_DFP_BWD, &e);
+  } else {
+    *tw = pow2 ? twiddle_table(p.N, TW_F32_STG, &e) : twiddle_table(p.N, ARITH_F32, &e);
+    if (dct) *tw2 = twiddle_table(p.M, ARITH_F32, &e);
+  }
+  return *tw && (!dct || *tw2);
+}
+
 bool fast_args(const PassParams& p, int arith, FastArgs* a, bool* row_in, bool* row_out) {
   const bool dct = p.mode == MODE_RE10 || p.mode == MODE_RE01;
   if ((p.mode != MODE_C2C && p.mode != MODE_R2C && p.mode != MODE_C2R && !dct) || p.nst == 0) return false;
@@ -164,12 +183,7 @@ bool fast_args(const PassParams& p, int arith, FastArgs* a, bool* row_in, bool* 
   a->out_df = p.out_df;
   a->mode = p.mode == MODE_C2C ? 0 : p.mode == MODE_R2C ? 1 : p.mode == MODE_C2R ? 2 : p.mode == MODE_RE10 ? 3 : 4;
   a->tw2 = nullptr;
-  if (dct) {  // Makhoul: the FFT runs on N points; the pre/post rotation uses the 4N table
-    cudaError_t e;
-    a->tw2 = p.tw;
-    a->tw = twiddle_table(p.N, arith, &e);
-    if (!a->tw) return false;
-  }
+  if (!fast_tables(p, arith, pow2, &a->tw, &a->tw2)) return false;
   a->Zi = p.Zi;
   a->Ni = p.Ni;
   a->Zo = p.Zo;
@@ -185,6 +199,19 @@ bool fast_args(const PassParams& p, int arith, FastArgs* a, bool* row_in, bool* 
   return true;
 }
 }  // namespace fast
+
+// Builds the tables a radix-8 / mixed-radix pass and its reverse direction
+// use (plans build them when created, so that executing allocates nothing).
+bool fast_pass_tables(const PassParams& p, int arith) {
+  fast::FastArgs a;
+  bool ri, ro;
+  PassParams q = p;
+  for (int sign : {-1, 1}) {
+    q.sign = sign;
+    fast::fast_args(q, arith, &a, &ri, &ro);
+  }
+  return true;
+}
 
 bool fast_pass_eligible(const PassParams& p, int arith) {
   fast::FastArgs a;

@@ -49,6 +49,13 @@ struct F32 {
   static __device__ __forceinline__ C lds(const S& s) { return s; }
   static __device__ __forceinline__ S sts(C v) { return v; }
   static __device__ __forceinline__ S twc(S w, int sign) { return sign < 0 ? w : make_float2(w.x, -w.y); }
+  // twiddles: the forward table W_M^m, conjugated for SIGN > 0
+  typedef float2 W;
+  static __device__ __forceinline__ W ldw(const void* base, int idx, int) { return __ldg((const W*)base + idx); }
+  template <int SIGN>
+  static __device__ __forceinline__ W twd(W w) {
+    return twc(w, SIGN);
+  }
   static __device__ __forceinline__ C conj(C a) { return make_float2(a.x, -a.y); }
   static __device__ __forceinline__ float c8() { return 0.70710678118654752440f; }
 };
@@ -94,35 +101,109 @@ __device__ __forceinline__ DD dd_mms(DD a, DD b, DD c, DD d) {
   return {s, e};
 }
 
+// Packed two-lane FP32 arithmetic (FADD2 / FMUL2 / FFMA2, sm_100 and
+// later): one instruction does the same operation on both floats of a pair,
+// so float-float complex arithmetic on the pairs (re, im) issues half the
+// instructions of its scalar form.  Negated operands are written as negated
+// pairs for the compiler to fold into the instruction.
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, neg2(b)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+// Float-float complex, packed: h = (re.hi, im.hi), l = (re.lo, im.lo).
+// Twiddles come from direction-specific tables (twiddle table kinds
+// TW_DFP_*) of two float4 per entry, w = wr + i wi:
+//   h = (wr.hi, wr.hi, -wi.hi, wi.hi), l = (wr.lo, wr.lo, -wi.lo, wi.lo),
+// the pairs of (re, im) = a (wr, wr) + swap(a) (-wi, wi), so no pair is built
+// at run time but the swapped operand; all h of a table come first, then
+// all l, so that a warp reading consecutive entries reads contiguous memory.
 struct FDD {
-  typedef float4 S;   // (re.hi, re.lo, im.hi, im.lo)
+  typedef float4 S;   // shared memory: (re.hi, im.hi, re.lo, im.lo)
   typedef double2 G;
-  struct C {
-    DD x, y;
+  struct W {
+    float4 h, l;
   };
-  static __device__ __forceinline__ C add(C a, C b) { return {dd_add(a.x, b.x), dd_add(a.y, b.y)}; }
-  static __device__ __forceinline__ C sub(C a, C b) { return {dd_sub(a.x, b.x), dd_sub(a.y, b.y)}; }
-  static __device__ __forceinline__ C mul(C a, S w) {
-    DD wr = {w.x, w.y}, wi = {w.z, w.w};
-    return {dd_mms(a.x, wr, a.y, wi), dd_mms(a.x, wi, dd_neg(a.y), wr)};
+  struct C {
+    float2 h, l;
+  };
+  // TwoSum on the high pairs, plain sums of the low pairs (unnormalised)
+  static __device__ __forceinline__ C add(C a, C b) {
+    const float2 s = add2(a.h, b.h);
+    const float2 bb = sub2(s, a.h);
+    const float2 e = add2(sub2(a.h, sub2(s, bb)), sub2(b.h, bb));
+    return {s, add2(add2(a.l, b.l), e)};
   }
-  static __device__ __forceinline__ C scal(C a, DD c) { return {dd_mulc(a.x, c), dd_mulc(a.y, c)}; }
-  static __device__ __forceinline__ C neg(C a) { return {dd_neg(a.x), dd_neg(a.y)}; }
-  static __device__ __forceinline__ C swap_neg_re(C a) { return {dd_neg(a.y), a.x}; }
-  static __device__ __forceinline__ C swap_neg_im(C a) { return {a.y, dd_neg(a.x)}; }
-  static __device__ __forceinline__ C renorm(C a) { return {dd_norm(a.x), dd_norm(a.y)}; }
+  // a + (-b) with the same steps
+  static __device__ __forceinline__ C sub(C a, C b) {
+    const float2 s = sub2(a.h, b.h);
+    const float2 bb = sub2(s, a.h);
+    const float2 e = sub2(sub2(a.h, sub2(s, bb)), add2(b.h, bb));
+    return {s, add2(sub2(a.l, b.l), e)};
+  }
+  static __device__ __forceinline__ C mul(C a, const W& w) {
+    const float2 sh = make_float2(a.h.y, a.h.x), sl = make_float2(a.l.y, a.l.x);
+    const float2 wr = make_float2(w.h.x, w.h.y), wi = make_float2(w.h.z, w.h.w);
+    const float2 wrl = make_float2(w.l.x, w.l.y), wil = make_float2(w.l.z, w.l.w);
+    const float2 P = mul2(a.h, wr);         // (x wr, y wr)
+    const float2 nEP = fma2(a.h, neg2(wr), P);  // minus its rounding error, exact
+    const float2 Q = mul2(sh, wi);          // (-y wi, x wi)
+    const float2 nEQ = fma2(sh, neg2(wi), Q);
+    const float2 s = add2(P, Q);
+    const float2 bb = sub2(s, P);
+    float2 e = add2(sub2(P, sub2(s, bb)), sub2(Q, bb));
+    e = sub2(sub2(e, nEP), nEQ);
+    e = fma2(a.h, wrl, e);
+    e = fma2(a.l, wr, e);
+    e = fma2(sh, wil, e);
+    e = fma2(sl, wi, e);
+    return {s, e};
+  }
+  // product with a real float-float constant, per component (scalar FMAs
+  // take the constant as an immediate)
+  static __device__ __forceinline__ C scal(C a, DD c) {
+    const DD x = dd_mulc(DD{a.h.x, a.l.x}, c), y = dd_mulc(DD{a.h.y, a.l.y}, c);
+    return {make_float2(x.hi, y.hi), make_float2(x.lo, y.lo)};
+  }
+  static __device__ __forceinline__ C neg(C a) {
+    return {make_float2(-a.h.x, -a.h.y), make_float2(-a.l.x, -a.l.y)};
+  }
+  static __device__ __forceinline__ C swap_neg_re(C a) {  // * i
+    return {make_float2(-a.h.y, a.h.x), make_float2(-a.l.y, a.l.x)};
+  }
+  static __device__ __forceinline__ C swap_neg_im(C a) {  // * (-i)
+    return {make_float2(a.h.y, -a.h.x), make_float2(a.l.y, -a.l.x)};
+  }
+  static __device__ __forceinline__ C renorm(C a) {
+    const float2 s = add2(a.h, a.l);
+    return {s, sub2(a.l, sub2(s, a.h))};
+  }
+  static __device__ __forceinline__ C from_df(df re, df im) {
+    return {make_float2(re.hi, im.hi), make_float2(re.lo, im.lo)};
+  }
+  static __device__ __forceinline__ df re_df(C v) { return df{v.h.x, v.l.x}; }
+  static __device__ __forceinline__ df im_df(C v) { return df{v.h.y, v.l.y}; }
   static __device__ __forceinline__ C ld(const G* p) {
     G v = *p;
-    df a = df_from_double(v.x), b = df_from_double(v.y);
-    return {{a.hi, a.lo}, {b.hi, b.lo}};
+    return from_df(df_from_double(v.x), df_from_double(v.y));
   }
   static __device__ __forceinline__ void st(G* p, C v) {
-    *p = make_double2(df_to_double(df{v.x.hi, v.x.lo}), df_to_double(df{v.y.hi, v.y.lo}));
+    *p = make_double2(df_to_double(re_df(v)), df_to_double(im_df(v)));
   }
-  static __device__ __forceinline__ C lds(const S& s) { return {{s.x, s.y}, {s.z, s.w}}; }
-  static __device__ __forceinline__ S sts(C v) { return make_float4(v.x.hi, v.x.lo, v.y.hi, v.y.lo); }
-  static __device__ __forceinline__ S twc(S w, int sign) { return sign < 0 ? w : make_float4(w.x, w.y, -w.z, -w.w); }
-  static __device__ __forceinline__ C conj(C a) { return {a.x, dd_neg(a.y)}; }
+  static __device__ __forceinline__ C lds(const S& s) { return {make_float2(s.x, s.y), make_float2(s.z, s.w)}; }
+  static __device__ __forceinline__ S sts(C v) { return make_float4(v.h.x, v.h.y, v.l.x, v.l.y); }
+  // entry idx of a table of cnt entries (high parts, then low parts)
+  static __device__ __forceinline__ W ldw(const void* base, int idx, int cnt) {
+    const float4* t = (const float4*)base;
+    return {__ldg(t + idx), __ldg(t + cnt + idx)};
+  }
+  // twiddle of direction SIGN: the tables are direction-specific already
+  template <int SIGN>
+  static __device__ __forceinline__ W twd(const W& w) {
+    return w;
+  }
+  static __device__ __forceinline__ C conj(C a) { return {make_float2(a.h.x, -a.h.y), make_float2(a.l.x, -a.l.y)}; }
   static __device__ __forceinline__ DD c8() {
     return {(float)0.70710678118654752440, (float)(0.70710678118654752440 - (double)(float)0.70710678118654752440)};
   }
@@ -207,6 +288,10 @@ __host__ __device__ constexpr int lsp_of() {
 
 __host__ __device__ constexpr int n8_of(int N) { return N >= 4096 ? 4 : (N >= 512 ? 3 : (N >= 64 ? 2 : 1)); }
 __host__ __device__ constexpr int pow8(int a) { return a == 4 ? 4096 : (a == 3 ? 512 : (a == 2 ? 64 : 8)); }
+// entries of the radix-8 kernel's stage-major twiddle table (fast_tw_count)
+__host__ __device__ constexpr int fast_tw_n(int N) {
+  return pow8(n8_of(N)) - 8 + (N / pow8(n8_of(N)) - 1) * pow8(n8_of(N));
+}
 
 struct FastArgs {
   const void* src;
@@ -259,13 +344,12 @@ template <>
 __device__ __forceinline__ F32::C gload<F32, true>(const F32::G* p, int) { return __ldcg(p); }
 template <bool CG>
 __device__ __forceinline__ FDD::C gload_fdd(const FDD::G* p, int isdf) {
-  if (isdf) {
+  if (isdf) {  // (re.hi, re.lo, im.hi, im.lo)
     float4 v = gld<CG>((const float4*)p);
-    return {{v.x, v.y}, {v.z, v.w}};
+    return {make_float2(v.x, v.z), make_float2(v.y, v.w)};
   }
   double2 v = gld<CG>(p);
-  df a = df_from_double(v.x), b = df_from_double(v.y);
-  return {{a.hi, a.lo}, {b.hi, b.lo}};
+  return FDD::from_df(df_from_double(v.x), df_from_double(v.y));
 }
 template <>
 __device__ __forceinline__ FDD::C gload<FDD, false>(const FDD::G* p, int df) { return gload_fdd<false>(p, df); }
@@ -279,7 +363,7 @@ template <>
 __device__ __forceinline__ void gstore<FDD>(FDD::G* p, FDD::C v, int df) {
   if (df) {
     FDD::C n = FDD::renorm(v);
-    *(float4*)p = make_float4(n.x.hi, n.x.lo, n.y.hi, n.y.lo);
+    *(float4*)p = make_float4(n.h.x, n.l.x, n.h.y, n.l.y);
   } else {
     FDD::st(p, v);
   }
@@ -298,13 +382,11 @@ __device__ __forceinline__ F32::C rload<F32, true>(const void* src, long long i)
 }
 template <>
 __device__ __forceinline__ FDD::C rload<FDD, false>(const void* src, long long i) {
-  df a = df_from_double(((const double*)src)[i]);
-  return {{a.hi, a.lo}, {0.f, 0.f}};
+  return FDD::from_df(df_from_double(((const double*)src)[i]), df{0.f, 0.f});
 }
 template <>
 __device__ __forceinline__ FDD::C rload<FDD, true>(const void* src, long long i) {
-  df a = df_from_double(__ldcg((const double*)src + i));
-  return {{a.hi, a.lo}, {0.f, 0.f}};
+  return FDD::from_df(df_from_double(__ldcg((const double*)src + i)), df{0.f, 0.f});
 }
 template <class P>
 __device__ __forceinline__ void rstore(void* dst, long long i, typename P::C v);
@@ -314,14 +396,14 @@ __device__ __forceinline__ void rstore<F32>(void* dst, long long i, F32::C v) {
 }
 template <>
 __device__ __forceinline__ void rstore<FDD>(void* dst, long long i, FDD::C v) {
-  ((double*)dst)[i] = df_to_double(df{v.x.hi, v.x.lo});
+  ((double*)dst)[i] = df_to_double(FDD::re_df(v));
 }
 template <class P>
 __device__ __forceinline__ typename P::C czero();
 template <>
 __device__ __forceinline__ F32::C czero<F32>() { return make_float2(0.f, 0.f); }
 template <>
-__device__ __forceinline__ FDD::C czero<FDD>() { return {{0.f, 0.f}, {0.f, 0.f}}; }
+__device__ __forceinline__ FDD::C czero<FDD>() { return {make_float2(0.f, 0.f), make_float2(0.f, 0.f)}; }
 
 // real input x_j of a real-to-real line (zero outside the embedded range)
 template <class P, bool CG>
@@ -342,7 +424,7 @@ __device__ __forceinline__ typename P::C load_elem(const FastArgs& a, long long 
     C xk = rx<P, CG>(a, off, e);
     C xm = e == 0 ? czero<P>() : rx<P, CG>(a, off, N - e);
     C z = P::sub(xk, P::swap_neg_re(xm));  // x_k - i x_(N-k)
-    return P::mul(z, P::twc(__ldg((const typename P::S*)a.tw2 + e), 1));
+    return P::mul(z, P::template twd<1>(P::ldw(a.tw2, e, 4 * N)));
   }
   bool mirror = false;
   int q, k = e;
@@ -364,7 +446,7 @@ template <class P, bool DCT = false>
 __device__ __forceinline__ void store_elem(const FastArgs& a, long long off, int e, typename P::C v, int N) {
   if constexpr (DCT) {
     if (a.mode == 3) {  // y_e = 2 Re(W_4N^e V_e)
-      v = P::mul(v, P::twc(__ldg((const typename P::S*)a.tw2 + e), -1));
+      v = P::mul(v, P::template twd<-1>(P::ldw(a.tw2, e, 4 * N)));
       v = P::add(v, v);
     } else {
       e = 2 * e < N ? 2 * e : 2 * (N - 1 - e) + 1;
@@ -458,7 +540,8 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
   const int l = ROW_IN ? tid / TPL : tid % L;
   const int t = ROW_IN ? tid % TPL : tid / L;
   const bool live = (g0 + l) < a.nlines;
-  const S* tw = (const S*)a.tw;
+  const void* tw = a.tw;  // stage-major table (TW_F32_STG, TW_DFP_*_STG)
+  constexpr int TWN = fast_tw_n(N);
   S* line = buf + l * LSP;
   bf8<P, SIGN>(v);  // stage 0 (Ns = 1, no twiddles)
   int Ns = 1;
@@ -477,9 +560,8 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
 #pragma unroll
     for (int r = 0; r < 8; r++) v[r] = P::lds(line[pad<P>(t + r * TPL)]);
     const int k = t % Ns;
-    const int step = N / (Ns * 8);
 #pragma unroll
-    for (int r = 1; r < 8; r++) v[r] = P::mul(v[r], P::twc(__ldg(&tw[k * r * step]), SIGN));
+    for (int r = 1; r < 8; r++) v[r] = P::mul(v[r], P::template twd<SIGN>(P::ldw(tw, Ns - 8 + (r - 1) * Ns + k, TWN)));
     bf8<P, SIGN>(v);
   }
   if (Q == 1) {
@@ -520,7 +602,7 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
 #pragma unroll
       for (int r = 0; r < Q; r++) {
         C x = P::lds(line[pad<P>(j + r * NQ)]);
-        if (r > 0) x = P::mul(x, P::twc(__ldg(&tw[j * r]), SIGN));
+        if (r > 0) x = P::mul(x, P::template twd<SIGN>(P::ldw(tw, NQ - 8 + (r - 1) * NQ + j, TWN)));
         w[b * Q + r] = x;
       }
       if (Q == 2) {
@@ -580,8 +662,15 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
   }
 }
 
+// resident CTAs per SM the register budget is fitted to: 1024 threads for
+// float-float (64 registers), no bound for FP32
+template <class P, int T>
+constexpr int fast_min_blocks() {
+  return sizeof(typename P::S) == 16 && T <= 1024 ? 1024 / T : 1;
+}
+
 template <class P, int SIGN, int N, int L, bool ROW_IN, bool ROW_OUT, int IO = 0>
-__global__ void __launch_bounds__(L*(N / 8)) k_fast(const FastArgs a) {
+__global__ void __launch_bounds__(L*(N / 8), (fast_min_blocks<P, L*(N / 8)>())) k_fast(const FastArgs a) {
   extern __shared__ __align__(16) unsigned char sm_raw[];
   fast_tile<P, SIGN, N, L, ROW_IN, ROW_OUT, false, IO>(a, blockIdx.x, sm_raw);
 }

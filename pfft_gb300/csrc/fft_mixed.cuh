@@ -115,7 +115,7 @@ struct MixedStage {
   }
 
   // twiddles and butterflies of this stage (inputs in v, outputs in place)
-  static __device__ __forceinline__ void compute(C* v, int t, const S* tw) {
+  static __device__ __forceinline__ void compute(C* v, int t, const void* tw) {
     constexpr int Ns = ns();
 #pragma unroll
     for (int i = 0; i < E / R; i++) {
@@ -124,7 +124,7 @@ struct MixedStage {
         const int k = b % Ns;
         constexpr int step = N / (Ns * R);
 #pragma unroll
-        for (int r = 1; r < R; r++) v[i * R + r] = P::mul(v[i * R + r], P::twc(__ldg(&tw[k * r * step]), SIGN));
+        for (int r = 1; r < R; r++) v[i * R + r] = P::mul(v[i * R + r], P::template twd<SIGN>(P::ldw(tw, k * r * step, N)));
       }
       bfR<P, SIGN, R>(v + i * R);
     }
@@ -140,7 +140,7 @@ struct MixedStage {
 };
 
 template <class P, int SIGN, int N, int E, int s>
-__device__ __forceinline__ void mixed_stages(typename P::C* v, int t, const typename P::S* tw, typename P::S* line) {
+__device__ __forceinline__ void mixed_stages(typename P::C* v, int t, const void* tw, typename P::S* line) {
   typedef MixedStage<P, SIGN, N, E, s> St;
   St::compute(v, t, tw);
   if constexpr (s + 1 < St::NS) {
@@ -196,7 +196,7 @@ __device__ __forceinline__ void mixed_tile(const FastArgs& a, long long blk, uns
   const int l = ROW_IN ? tid / TPL : tid % L;
   const int t = ROW_IN ? tid % TPL : tid / L;
   const bool live = (g0 + l) < a.nlines;
-  const S* tw = (const S*)a.tw;
+  const void* tw = a.tw;  // natural-order table of N entries
   S* line = buf + l * LSP;
 
   // plain c2c lines only (fast_args sends no other mode here)

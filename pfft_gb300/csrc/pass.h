@@ -11,6 +11,26 @@
 namespace pg {
 
 enum ArithId { ARITH_F32 = 0, ARITH_F64 = 1, ARITH_DF = 2 };
+// Twiddle table kinds besides the arithmetic ids (one table per length and
+// kind, twiddle.cpp):
+//   TW_DFP_FWD / _BWD: packed float-float tables of the mixed-radix kernel
+//     and of the DCT rotations, entry m = W_M^(+-m) in natural order;
+//   TW_F32_STG, TW_DFP_FWD_STG / _BWD_STG: the radix-8 kernel's tables in
+//     stage-major order (fast_tw_count entries): radix-8 stage s (Ns = 8^s)
+//     holds W_N^(k r N/(8 Ns)) at Ns - 8 + (r-1) Ns + k (r = 1..7,
+//     k < Ns), the final radix-q stage (q = 2, 4) holds W_N^(j r) at
+//     P - 8 + (r-1) N/q + j (P the last power of 8 dividing N), so a warp's
+//     threads (consecutive k or j) read consecutive entries.
+// Packed tables are stored as two arrays of float4: all high parts, then all
+// low parts (FDD::W).
+enum TwiddleKind { TW_DFP_FWD = 16, TW_DFP_BWD = 17, TW_F32_STG = 18, TW_DFP_FWD_STG = 19, TW_DFP_BWD_STG = 20 };
+// entries of a stage-major table for a power-of-two N >= 16
+inline int fast_tw_count(int N) {
+  int p8 = 8;
+  while (p8 * 8 <= N) p8 *= 8;
+  const int q = N / p8;
+  return p8 - 8 + (q - 1) * (N / q);
+}
 
 // How the logical length-N input line is turned into the length-M complex
 // sequence in shared memory, and how the output line is read back.
@@ -87,6 +107,8 @@ int launch_pass(const PassParams& p, int arith, cudaStream_t stream);
 int kernel_path();
 // true when launch_pass runs this pass on the register-resident radix-8 kernel
 bool fast_pass_eligible(const PassParams& p, int arith);
+// builds the twiddle tables of a radix-8 / mixed-radix pass, both directions
+bool fast_pass_tables(const PassParams& p, int arith);
 void set_kernel_path(int v);
 // staged persistent variant of the radix-8 kernel for plain c2c passes:
 // 1 per pass as PassParams::staged says (default), 2 wherever the layout

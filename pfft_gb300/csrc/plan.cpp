@@ -158,7 +158,9 @@ Plan* make_plan(const PlanDesc& base, void* in, void* out) {
   // pre-build twiddle tables so that execution allocates nothing
   for (const Pass& ps : pl->fwd.passes) {
     cudaError_t e;
-    if (!twiddle_table(ps.p.M, pl->arith, &e) || !twiddle_table(ps.p.N, pl->arith, &e)) {
+    bool ok = twiddle_table(ps.p.M, pl->arith, &e) && twiddle_table(ps.p.N, pl->arith, &e);
+    if (ok && pl->arith != ARITH_F64) fast_pass_tables(ps.p, pl->arith);  // radix-8 / mixed-radix tables
+    if (!ok) {
       cuda_check(e, "twiddle table");
       destroy_plan(pl);
       return nullptr;

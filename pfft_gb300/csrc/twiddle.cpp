@@ -1,4 +1,5 @@
-// Twiddle tables W_M^m = exp(-2*pi*i*m/M), m < M, one per (M, arithmetic).
+// Twiddle tables W_M^m = exp(-2*pi*i*m/M), m < M, one per (M, arithmetic),
+// and the tables of the radix-8 / mixed-radix kernels (kinds in pass.h).
 // Computed once on the host in long double (octant-folded argument) and kept
 // in device memory until pfft_cleanup().
 #include <math.h>
@@ -47,27 +48,72 @@ void cis(long long k, long long M, long double* c, long double* s) {
 }
 }  // namespace
 
+namespace {
+// packed float-float entry of w = c + i s: high pair (c, c, -s, s) into h,
+// low pair into l
+void packed_entry(long double c, long double s, float* h, float* l) {
+  const float rh = (float)c, ih = (float)s;
+  const float rl = (float)(c - (long double)rh), il = (float)(s - (long double)ih);
+  h[0] = rh; h[1] = rh; h[2] = -ih; h[3] = ih;
+  l[0] = rl; l[1] = rl; l[2] = -il; l[3] = il;
+}
+}  // namespace
+
 const void* twiddle_table(int M, int arith, cudaError_t* err) {
   std::lock_guard<std::mutex> lk(g_mu);
   auto key = std::make_pair(M, arith);
   auto it = g_tables.find(key);
   if (it != g_tables.end()) return it->second;
-  size_t esz = arith_sm_bytes(arith);
-  std::vector<unsigned char> host((size_t)M * esz);
-  for (int m = 0; m < M; m++) {
+  const bool staged = arith == TW_F32_STG || arith == TW_DFP_FWD_STG || arith == TW_DFP_BWD_STG;
+  const bool packed = arith == TW_DFP_FWD || arith == TW_DFP_BWD || arith == TW_DFP_FWD_STG || arith == TW_DFP_BWD_STG;
+  const bool bwd = arith == TW_DFP_BWD || arith == TW_DFP_BWD_STG;
+  if (staged && (M < 16 || (M & (M - 1)))) {
+    if (err) *err = cudaErrorInvalidValue;
+    return nullptr;
+  }
+  // entry j of the table: exponent m of W_M^m
+  std::vector<long long> expo;
+  if (staged) {
+    int p8 = 8;
+    while (p8 * 8 <= M) p8 *= 8;
+    const int q = M / p8;
+    for (int Ns = 8; Ns < p8; Ns *= 8)
+      for (int r = 1; r < 8; r++)
+        for (int k = 0; k < Ns; k++) expo.push_back((long long)k * r * (M / (Ns * 8)));
+    for (int r = 1; r < q; r++)
+      for (int j = 0; j < M / q; j++) expo.push_back((long long)j * r);
+  } else {
+    for (int m = 0; m < M; m++) expo.push_back(m);
+  }
+  const size_t n = expo.size();
+  size_t bytes;
+  if (packed)
+    bytes = n * 32;
+  else if (arith == ARITH_F32 || arith == TW_F32_STG)
+    bytes = n * 8;
+  else
+    bytes = n * (size_t)arith_sm_bytes(arith);
+  std::vector<unsigned char> host(bytes > 0 ? bytes : 16);
+  for (size_t j = 0; j < n; j++) {
     long double c, s;
-    cis(m, M, &c, &s);
+    cis(expo[j], M, &c, &s);
     s = -s;  // forward direction
-    if (arith == ARITH_F32) {
+    if (packed) {
+      if (bwd) s = -s;
+      float h[4], l[4];
+      packed_entry(c, s, h, l);
+      memcpy(&host[j * 16], h, 16);
+      memcpy(&host[(n + j) * 16], l, 16);
+    } else if (arith == ARITH_F32 || arith == TW_F32_STG) {
       float v[2] = {(float)c, (float)s};
-      memcpy(&host[(size_t)m * esz], v, 8);
+      memcpy(&host[j * 8], v, 8);
     } else if (arith == ARITH_F64) {
       double v[2] = {(double)c, (double)s};
-      memcpy(&host[(size_t)m * esz], v, 16);
+      memcpy(&host[j * 16], v, 16);
     } else {
       float ch = (float)c, sh = (float)s;
       float v[4] = {ch, (float)(c - (long double)ch), sh, (float)(s - (long double)sh)};
-      memcpy(&host[(size_t)m * esz], v, 16);
+      memcpy(&host[j * 16], v, 16);
     }
   }
   void* d = nullptr;
