@@ -93,7 +93,13 @@ int pfft_gb300_selftest_df_roundtrip(const double *in, double *out, long long n,
  *      FP32 rate on GB300)
  *   2  by size (default): native FP64 for transforms of at most 2^18 points
  *      (howmany included), float-float above.
- * The environment variable PFFT_GB300_F64_ARITH=df|native|auto sets the
+ *   3  float-float whose power-of-two c2c passes on the radix-8 kernel round
+ *      the high words of each radix-8 butterfly to a common grid, so that the
+ *      butterfly's additions are exact without TwoSum: fewer FP32
+ *      operations, relative L2 error about 1e-13 per pass (bounded by a
+ *      small multiple of 2^-45 per radix-8 stage, relative to the data's L2
+ *      norm); other passes as in mode 0.
+ * The environment variable PFFT_GB300_F64_ARITH=df|native|auto|dfq sets the
  * initial mode.  Returns 0, or -1 for an unknown mode. */
 int pfft_gb300_set_double_arith(int mode);
 int pfft_gb300_get_double_arith(void);

@@ -424,7 +424,7 @@ int pfft_gb300_staged_status(void) {
   return e == cudaSuccess ? (h ? 1 : 0) : -(int)e;
 }
 int pfft_gb300_set_double_arith(int mode) {
-  if (mode != DARITH_DF && mode != DARITH_NATIVE && mode != DARITH_AUTO) return -1;
+  if (mode != DARITH_DF && mode != DARITH_NATIVE && mode != DARITH_AUTO && mode != DARITH_DFQ) return -1;
   set_double_arith(mode);
   return 0;
 }

@@ -140,6 +140,7 @@ struct TimerData {
 struct Plan {
   PlanDesc d;
   int arith = ARITH_DF;
+  int quant = 0;        // float-float: block-quantised radix-8 stages (PassParams::quant)
   void* in = nullptr;   // planned arrays
   void* out = nullptr;
   bool inplace = false;
@@ -189,7 +190,7 @@ void execute_plan(Plan* pl, void* in, void* out, bool adjoint);
 void destroy_plan(Plan* pl);
 
 // arithmetic policy of the double API: float-float, native FP64, or by size
-enum { DARITH_DF = 0, DARITH_NATIVE = 1, DARITH_AUTO = 2 };
+enum { DARITH_DF = 0, DARITH_NATIVE = 1, DARITH_AUTO = 2, DARITH_DFQ = 3 };
 constexpr long long DARITH_AUTO_POINTS = 1LL << 18;
 int double_arith();
 void set_double_arith(int a);

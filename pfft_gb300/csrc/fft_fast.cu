@@ -258,6 +258,11 @@ int launch_fast_pass(const PassParams& p, int arith, cudaStream_t stream) {
       return big ? launch_large<F32, -1>(N, a, row_in, row_out, stream) : launch_small<F32, -1>(N, a, row_in, row_out, stream);
     return big ? launch_large<F32, 1>(N, a, row_in, row_out, stream) : launch_small<F32, 1>(N, a, row_in, row_out, stream);
   }
+  if (p.quant) {  // block-quantised float-float radix-8 stages
+    if (sign < 0)
+      return big ? launch_large<FQ, -1>(N, a, row_in, row_out, stream) : launch_small<FQ, -1>(N, a, row_in, row_out, stream);
+    return big ? launch_large<FQ, 1>(N, a, row_in, row_out, stream) : launch_small<FQ, 1>(N, a, row_in, row_out, stream);
+  }
   if (sign < 0)
     return big ? launch_large<FDD, -1>(N, a, row_in, row_out, stream) : launch_small<FDD, -1>(N, a, row_in, row_out, stream);
   return big ? launch_large<FDD, 1>(N, a, row_in, row_out, stream) : launch_small<FDD, 1>(N, a, row_in, row_out, stream);

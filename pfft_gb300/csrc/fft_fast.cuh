@@ -21,6 +21,7 @@
 // A length N = 8^a * q (q = 1, 2, 4) runs a radix-8 stages and one radix-q stage.
 #pragma once
 #include <algorithm>
+#include <type_traits>
 #include "arith.cuh"
 #include "pass.h"
 #include "tma.cuh"
@@ -262,6 +263,91 @@ __device__ __forceinline__ void bf8(typename P::C* v) {
   v[7] = P::sub(e3, o3);
 }
 
+// ---- block-quantised float-float radix-8 butterflies -----------------------------
+// FQ: float-float values whose high words are rounded, before each radix-8
+// butterfly, to a grid common to the butterfly, so that every addition of
+// high words inside it is exact and needs no TwoSum (2 packed operations per
+// complex addition instead of 8).  With m the largest high word of the
+// butterfly's 16 components, m < 2^(T-4), the grid is q = 2^(T-24): every
+// partial sum of the butterfly is bounded by (4 + 4 sqrt 2) m < 2^T (the
+// sqrt(1/2) products included), so every sum of grid points is a float.
+// Rounding h to the grid adds h - round(h) (|.| <= q/2) to the low word, whose
+// own rounding is then 2^-24 of a larger low word: the error of a stage is
+// about 2^-45 of the butterfly's largest component (relative L2 error about
+// 1e-13 per 512-point pass on uniform data, against 1e-14 for the TwoSum
+// form).  Loads, stores, twiddle products and the radix-2/4 stage are those
+// of FDD.
+struct FQ : FDD {};
+
+// h rounded to the grid of c (c = 1.5 * 2^(T-1) or 1.5 * 2^T: ulp(c) = q or
+// 2q), the difference moved to the low word
+__device__ __forceinline__ FDD::C fq_round(FDD::C a, float2 c) {
+  const float2 hq = sub2(add2(a.h, c), c);
+  return {hq, add2(a.l, sub2(a.h, hq))};
+}
+__device__ __forceinline__ FDD::C fq_add(FDD::C a, FDD::C b) { return {add2(a.h, b.h), add2(a.l, b.l)}; }
+__device__ __forceinline__ FDD::C fq_sub(FDD::C a, FDD::C b) { return {sub2(a.h, b.h), sub2(a.l, b.l)}; }
+// sqrt(1/2) * a (exact product of the high words: value + error), high word
+// back on the grid with c2 = 1.5 * 2^T (|product| <= 4 sqrt 2 m < 2^(T-1.5))
+__device__ __forceinline__ FDD::C fq_c8(FDD::C a, float2 c2) {
+  constexpr double k = 0.70710678118654752440;
+  const float2 ch = make_float2((float)k, (float)k);
+  const float2 cl = make_float2((float)(k - (double)(float)k), (float)(k - (double)(float)k));
+  const float2 p = mul2(a.h, ch);
+  float2 e = fma2(a.h, ch, neg2(p));
+  e = fma2(a.h, cl, e);
+  e = fma2(a.l, ch, e);
+  const float2 pq = sub2(add2(p, c2), c2);
+  return {pq, add2(e, sub2(p, pq))};
+}
+template <int SIGN>
+__device__ __forceinline__ void fq_bf4(FDD::C& a0, FDD::C& a1, FDD::C& a2, FDD::C& a3) {
+  FDD::C t0 = fq_add(a0, a2), t1 = fq_sub(a0, a2);
+  FDD::C t2 = fq_add(a1, a3), t3 = msi<FDD, SIGN>(fq_sub(a1, a3));
+  a0 = fq_add(t0, t2);
+  a2 = fq_sub(t0, t2);
+  a1 = fq_add(t1, t3);
+  a3 = fq_sub(t1, t3);
+}
+// in-place radix-8 DFT of unnormalised float-float values (natural order)
+template <int SIGN>
+__device__ __forceinline__ void bf8q(FDD::C* v) {
+  float m = fmaxf(fabsf(v[0].h.x), fabsf(v[0].h.y));
+#pragma unroll
+  for (int r = 1; r < 8; r++) m = fmaxf(m, fmaxf(fabsf(v[r].h.x), fabsf(v[r].h.y)));
+  // m < 2^(e-126) for the biased exponent e of m: T = e - 122; the clamp keeps
+  // c2 finite (magnitudes near the float limit overflow the sums anyway)
+  const unsigned eb = min(__float_as_uint(m) & 0x7F800000u, 249u << 23);
+  const float c1s = __uint_as_float(eb + (4u << 23) + 0x400000u);  // 1.5 * 2^(T-1)
+  const float c2s = __uint_as_float(eb + (5u << 23) + 0x400000u);  // 1.5 * 2^T
+  const float2 c1 = make_float2(c1s, c1s), c2 = make_float2(c2s, c2s);
+#pragma unroll
+  for (int r = 0; r < 8; r++) v[r] = fq_round(v[r], c1);
+  fq_bf4<SIGN>(v[0], v[2], v[4], v[6]);
+  fq_bf4<SIGN>(v[1], v[3], v[5], v[7]);
+  // W8^1 z = c (z + S i z);  W8^3 z = c (S i z - z)
+  const FDD::C o1 = fq_c8(fq_add(v[3], msi<FDD, SIGN>(v[3])), c2);
+  const FDD::C o3 = fq_c8(fq_sub(msi<FDD, SIGN>(v[7]), v[7]), c2);
+  const FDD::C o2 = msi<FDD, SIGN>(v[5]);
+  const FDD::C e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6], o0 = v[1];
+  v[0] = fq_add(e0, o0);
+  v[4] = fq_sub(e0, o0);
+  v[1] = fq_add(e1, o1);
+  v[5] = fq_sub(e1, o1);
+  v[2] = fq_add(e2, o2);
+  v[6] = fq_sub(e2, o2);
+  v[3] = fq_add(e3, o3);
+  v[7] = fq_sub(e3, o3);
+}
+// the radix-8 butterfly of a policy
+template <class P, int SIGN>
+__device__ __forceinline__ void bf8x(typename P::C* v) {
+  if constexpr (std::is_same<P, FQ>::value)
+    bf8q<SIGN>(v);
+  else
+    bf8<P, SIGN>(v);
+}
+
 // Shared-memory layout of a tile: L lines at stride lsp_of, element p of a
 // line at index pad(p).  The layouts below make every stage exchange of the
 // kernel free of bank conflicts; they were chosen by simulating the
@@ -355,6 +441,10 @@ template <>
 __device__ __forceinline__ FDD::C gload<FDD, false>(const FDD::G* p, int df) { return gload_fdd<false>(p, df); }
 template <>
 __device__ __forceinline__ FDD::C gload<FDD, true>(const FDD::G* p, int df) { return gload_fdd<true>(p, df); }
+template <>
+__device__ __forceinline__ FDD::C gload<FQ, false>(const FDD::G* p, int df) { return gload_fdd<false>(p, df); }
+template <>
+__device__ __forceinline__ FDD::C gload<FQ, true>(const FDD::G* p, int df) { return gload_fdd<true>(p, df); }
 template <class P>
 __device__ __forceinline__ void gstore(typename P::G* p, typename P::C v, int df);
 template <>
@@ -367,6 +457,10 @@ __device__ __forceinline__ void gstore<FDD>(FDD::G* p, FDD::C v, int df) {
   } else {
     FDD::st(p, v);
   }
+}
+template <>
+__device__ __forceinline__ void gstore<FQ>(FDD::G* p, FDD::C v, int df) {
+  gstore<FDD>(p, v, df);
 }
 
 // real-array element access (r2c input, c2r output)
@@ -543,7 +637,7 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
   const void* tw = a.tw;  // stage-major table (TW_F32_STG, TW_DFP_*_STG)
   constexpr int TWN = fast_tw_n(N);
   S* line = buf + l * LSP;
-  bf8<P, SIGN>(v);  // stage 0 (Ns = 1, no twiddles)
+  bf8x<P, SIGN>(v);  // stage 0 (Ns = 1, no twiddles)
   int Ns = 1;
   // radix-8 stages 1 .. NS8-1 through shared memory
 #pragma unroll
@@ -562,7 +656,7 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
     const int k = t % Ns;
 #pragma unroll
     for (int r = 1; r < 8; r++) v[r] = P::mul(v[r], P::template twd<SIGN>(P::ldw(tw, Ns - 8 + (r - 1) * Ns + k, TWN)));
-    bf8<P, SIGN>(v);
+    bf8x<P, SIGN>(v);
   }
   if (Q == 1) {
     // v holds the last stage (Ns = N/8, k = t): outputs y[t + r*TPL]

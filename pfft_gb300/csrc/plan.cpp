@@ -62,6 +62,7 @@ int double_arith() {
     const char* e = getenv("PFFT_GB300_F64_ARITH");
     g_double_arith = (e && strcmp(e, "native") == 0) ? DARITH_NATIVE
                      : (e && strcmp(e, "df") == 0)   ? DARITH_DF
+                     : (e && strcmp(e, "dfq") == 0)  ? DARITH_DFQ
                                                      : DARITH_AUTO;
   }
   return g_double_arith;
@@ -75,10 +76,17 @@ void set_double_arith(int a) { g_double_arith = a; }
 int plan_double_arith(const PlanDesc& d) {
   const int m = double_arith();
   if (m == DARITH_NATIVE) return ARITH_F64;
-  if (m == DARITH_DF) return ARITH_DF;
+  if (m == DARITH_DF || m == DARITH_DFQ) return ARITH_DF;
   double pts = (double)d.howmany;
   for (int t = 0; t < d.rnk_n; t++) pts *= (double)d.n[t];
   return pts <= (double)DARITH_AUTO_POINTS ? ARITH_F64 : ARITH_DF;
+}
+
+// Block-quantised float-float radix-8 stages (fft_fast.cuh, FQ) for the
+// plain power-of-two c2c passes of a float-float plan: chosen with the
+// double-arithmetic mode DARITH_DFQ.
+static void mark_quant(const Plan* pl, PassProgram* prog) {
+  for (Pass& ps : prog->passes) ps.p.quant = pl->quant;
 }
 
 // ---- plans -------------------------------------------------------------------
@@ -139,6 +147,7 @@ Plan* make_plan(const PlanDesc& base, void* in, void* out) {
   Plan* pl = new Plan();
   pl->d = base;
   pl->arith = base.prec == 0 ? ARITH_F32 : plan_double_arith(base);
+  pl->quant = (pl->arith == ARITH_DF && double_arith() == DARITH_DFQ) ? 1 : 0;
   pl->in = in;
   pl->out = out;
   pl->inplace = (in == out) && in != nullptr;
@@ -146,6 +155,7 @@ Plan* make_plan(const PlanDesc& base, void* in, void* out) {
     delete pl;
     return nullptr;
   }
+  mark_quant(pl, &pl->fwd);
   if (!ensure_workspace(pl, pl->fwd)) {
     destroy_plan(pl);
     return nullptr;
@@ -217,6 +227,7 @@ void execute_plan(Plan* pl, void* in, void* out, bool adjoint) {
       report("adjoint not available for this plan");
       return;
     }
+    mark_quant(pl, &pl->adj);
     if (!ensure_workspace(pl, pl->adj)) return;
     apply_wisdom(&pl->adj, pl->arith);
     if ((pl->d.pfft_flags & (F_PATIENT | F_EXHAUSTIVE | F_TUNE)) && !tune_program(pl, &pl->adj)) return;

@@ -86,9 +86,10 @@ def comm_for(req):
 class double_arith:
     """Context manager selecting the double API's arithmetic for the plans
     created inside it: "double" keeps the default (by size), "double-df" forces
-    float-float, "double-f64" native FP64; "float" changes nothing."""
+    float-float, "double-f64" native FP64, "double-dfq" float-float with
+    block-quantised radix-8 stages; "float" changes nothing."""
 
-    MODES = {"double-df": 0, "double-f64": 1}
+    MODES = {"double-df": 0, "double-f64": 1, "double-dfq": 3}
 
     def __init__(self, prec):
         self.mode = self.MODES.get(prec)
@@ -113,8 +114,8 @@ def is_double(prec):
 def gpu_run(req, x, prec="double", inplace=False, adjoint=False, torch=None, keep=False):
     """Plan + execute through the C-ABI with device arrays; returns float64
     numpy of the output layout (the adjoint maps the output layout to the
-    input layout).  prec: "float", "double" (default arithmetic), "double-df"
-    or "double-f64"."""
+    input layout).  prec: "float", "double" (default arithmetic), "double-df",
+    "double-dfq" or "double-f64"."""
     import torch as _t
     torch = torch or _t
     L = pg.lib()

@@ -105,6 +105,13 @@ def test_c5_512cube_complex128_roundtrip(cuda, pfft_lib):
     assert rt <= 1e-12 and pv <= 1e-12, (rt, pv)
 
 
+def test_c5_512cube_complex128_roundtrip_block_quantised(cuda, pfft_lib):
+    """512^3 complex128 with block-quantised float-float radix-8 stages."""
+    with double_arith("double-dfq"):
+        rt, pv = _roundtrip_large(cuda, (512, 512, 512), "double")
+    assert rt <= 1e-12 and pv <= 1e-12, (rt, pv)
+
+
 def test_c5_1024cube_complex64_roundtrip(cuda, pfft_lib):
     rt, pv = _roundtrip_large(cuda, (1024, 1024, 1024), "float")
     assert rt <= 2e-6 and pv <= 2e-6, (rt, pv)

@@ -7,8 +7,9 @@ r2r kinds they use, plus the configurations of the benchmark suite at sizes
 the oracle finishes in seconds.  Tolerances: relative L2 <= 1e-12 for the
 double API, <= 2e-6 for the float API.  The double API is run with its
 default arithmetic ("double": native FP64 up to 2^18 points, float-float
-above) and with float-float forced ("double-df"), so both arithmetics are
-checked at every size.
+above), with float-float forced ("double-df") and with float-float whose
+radix-8 stages round the high words to a per-butterfly grid ("double-dfq"),
+so every arithmetic is checked at every size.
 """
 import numpy as np
 import pytest
@@ -18,9 +19,9 @@ from tests.pfft_util import Req, gpu_run, mask_padding, oracle_run, random_input
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"double": 1e-12, "double-df": 1e-12, "double-f64": 1e-12, "float": 2e-6}
-PRECS = ["double", "double-df", "float"]
-DPRECS = ["double", "double-df"]
+TOL = {"double": 1e-12, "double-df": 1e-12, "double-dfq": 1e-12, "double-f64": 1e-12, "float": 2e-6}
+PRECS = ["double", "double-df", "double-dfq", "float"]
+DPRECS = ["double", "double-df", "double-dfq"]
 TO, TI = pg.PFFT_TRANSPOSED_OUT, pg.PFFT_TRANSPOSED_IN
 PAD = pg.PFFT_PADDED_R2C
 
@@ -51,7 +52,7 @@ def test_c2c_3d(cuda, pfft_lib, n, flags, prec):
 
 
 @pytest.mark.parametrize("sign", [-1, 1])
-@pytest.mark.parametrize("prec", ["double", "double-df"])
+@pytest.mark.parametrize("prec", DPRECS)
 def test_c2c_backward_and_inplace(cuda, pfft_lib, sign, prec):
     check(Req("c2c", (29, 27, 31), sign=sign), prec, inplace=True)
     check(Req("c2c", (29, 27, 31), sign=sign, flags=TO), prec, inplace=True)
@@ -168,9 +169,32 @@ def test_double_arith_modes(cuda, pfft_lib):
     """Mode selection: unknown modes are refused, the previous mode stays."""
     L = pg.lib()
     old = L.pfft_gb300_get_double_arith()
-    assert old in (0, 1, 2)
+    assert old in (0, 1, 2, 3)
     assert L.pfft_gb300_set_double_arith(7) == -1
     assert L.pfft_gb300_get_double_arith() == old
+
+
+@pytest.mark.parametrize("n,flags", [((16, 512, 8), 0), ((512, 4, 64), TO), ((8, 16, 4096), 0), ((4, 1024, 8), TI),
+                                     ((128, 32, 256), 0), ((2048, 8, 16), TO)])
+@pytest.mark.parametrize("sign", [-1, 1])
+def test_block_quantised_error_level(cuda, pfft_lib, n, flags, sign):
+    """The block-quantised float-float radix-8 stages ("double-dfq") stay
+    within a few times 1e-13 relative L2 per pass on uniform and normal data
+    and on data spanning 2^-30..2^30 in magnitude (the error is relative to
+    each butterfly's largest component), against about 1e-14 for TwoSum
+    float-float on the same lines."""
+    req = Req("c2c", n, flags=flags, sign=sign)
+    rng = np.random.default_rng(5)
+    for dist in ("uniform", "normal", "wide"):
+        if dist == "wide":
+            x = rng.standard_normal(2 * int(np.prod(n))) * np.exp2(rng.uniform(-30, 30, 2 * int(np.prod(n))))
+        else:
+            x = random_input(req, rng, dist)
+        ref = oracle_run(req, x)
+        eq = rel_l2(gpu_run(req, x, prec="double-dfq"), ref)
+        ed = rel_l2(gpu_run(req, x, prec="double-df"), ref)
+        print("dfq %s %s %s: %.3e (df %.3e)" % (n, sign, dist, eq, ed))
+        assert eq <= 1e-12 and ed <= 1e-13, (dist, eq, ed)
 
 
 @pytest.mark.parametrize("n,flags", [((32, 32, 32), 0), ((16, 32, 64), TO), ((64, 64, 64), 0), ((128, 64, 256), TO),
