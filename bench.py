@@ -19,6 +19,10 @@ needed between steps).
   cpu_baseline  the CPU oracle (a C FP64 port, not the reference, which cannot
           be built: it needs FFTW-MPI and MPI) on the host cores, on a bounded
           sample of the same workload
+  accuracy  round-trip relative L2 error (backward of the measured forward
+          output, divided by N, against the input) and the Parseval defect of
+          the measured transform; the double API's arithmetic is its default
+          (float-float with block-quantised radix-8 stages at this size)
 
 --impl reference times that CPU port instead (the reference arm).
 With --gpus N > 1 (torchrun), every rank runs an independent replica (the path
@@ -378,6 +382,7 @@ def main():
     npass = ctypes.c_int(0)
     getattr(L, pre + "gb300_plan_info")(plan, ctypes.byref(npass), None, None)
     plan_arith = getattr(L, pre + "gb300_plan_arith")(plan)
+    dmode = L.pfft_gb300_get_double_arith()
     pass_bytes = []
     pass_kernel = [getattr(L, pre + "gb300_pass_kernel")(plan, i) for i in range(npass.value)]
     for i in range(npass.value):
@@ -432,6 +437,23 @@ def main():
             getattr(L, pre + "execute_dft")(plan, hin.data_ptr(), hout.data_ptr())
         e2e_s = (time.perf_counter() - t0) / args.e2e_steps
         e2e_max = reduce_max(e2e_s, world)
+    # ---- accuracy of the measured transform (size-independent properties) ----
+    # b holds forward(a): backward with a second plan, round-trip error
+    # |backward(forward(a))/N - a| / |a| and Parseval |forward(a)|^2 / N vs |a|^2
+    c = torch.empty_like(a)
+    pb = getattr(L, pre + "plan_dft_3d")(pg.ints(n), b.data_ptr(), c.data_ptr(), comm, pg.PFFT_BACKWARD,
+                                         pg.PFFT_TRANSPOSED_NONE | pg.PFFT_MEASURE)
+    accuracy = None
+    if pb:
+        getattr(L, pre + "execute")(pb)
+        torch.cuda.synchronize()
+        na = float(torch.linalg.vector_norm(a.double()))
+        nb = float(torch.linalg.vector_norm(b.double()))
+        accuracy = {"roundtrip_rel_l2": float(torch.linalg.vector_norm(c.double() / cnt - a.double())) / na,
+                    "parseval_rel": abs(nb * nb / cnt - na * na) / (na * na),
+                    "bound": 1e-12 if args.prec == "double" else 2e-6}
+        getattr(L, pre + "destroy_plan")(pb)
+    del c
     getattr(L, pre + "destroy_plan")(plan)
     del a, b
     torch.cuda.empty_cache()
@@ -459,7 +481,9 @@ def main():
         "metric": "3D FFT HBM GB/s & %roofline, 5N*log2N GFLOP/s; batched vs loop; adjoint cost",
         "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": {0: "f32", 1: "f64", 2: "f64 storage, float-float arithmetic"}[plan_arith],
+        "dtype": {0: "f32", 1: "f64", 2: "f64 storage, float-float arithmetic" +
+                  (" (block-quantised radix-8 stages)" if dmode in (2, 3) else " (TwoSum)")}[plan_arith],
+        "accuracy": accuracy,
         "data": "synthetic uniform[-1,1) seed 1+rank",
         "config": {"workload": "pfft_execute c2c %s %s forward, 1x1 procmesh, out-of-place, "
                                "TRANSPOSED_NONE" % ("x".join(map(str, n)) if args.shape else "%d^3" % args.n,

@@ -86,17 +86,23 @@ int pfft_gb300_batch_wait_selftest(long long spin_limit);
  * API's kernels, element by element (device arrays, queued on `stream`). */
 int pfft_gb300_selftest_df_roundtrip(const double *in, double *out, long long n, void *stream);
 
+/* Test hook: the fast path of the float-float -> double conversion against
+ * the full routine on n device float pairs (hi, lo).  counts: two zeroed
+ * device words that receive the number of values the fast path took and how
+ * many of its results differ from the full routine's. */
+int pfft_gb300_selftest_df_fast(const float *pairs, long long n, unsigned long long *counts, void *stream);
+
 /* Arithmetic of the double API, for plans created afterwards:
- *   0  float-float on the FP32 pipes (48-49 significant bits; relative L2
- *      error of a transform about 1e-15)
+ *   0  float-float on the FP32 pipes with TwoSum additions (48-49
+ *      significant bits; relative L2 error of a transform about 1e-14)
  *   1  native FP64 (full double rounding; FP64 issues at about 1/64 of the
  *      FP32 rate on GB300)
  *   2  by size (default): native FP64 for transforms of at most 2^18 points
- *      (howmany included), float-float above.
+ *      (howmany included), mode 3 above.
  *   3  float-float whose power-of-two c2c passes on the radix-8 kernel round
  *      the high words of each radix-8 butterfly to a common grid, so that the
  *      butterfly's additions are exact without TwoSum: fewer FP32
- *      operations, relative L2 error about 1e-13 per pass (bounded by a
+ *      operations, relative L2 error about 2e-13 per pass (bounded by a
  *      small multiple of 2^-45 per radix-8 stage, relative to the data's L2
  *      norm); other passes as in mode 0.
  * The environment variable PFFT_GB300_F64_ARITH=df|native|auto|dfq sets the

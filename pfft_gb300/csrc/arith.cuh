@@ -137,6 +137,53 @@ __device__ __forceinline__ double df_to_double(df v) {
   return __longlong_as_double((long long)P);
 }
 
+// Fast path of float-float -> double, bit-identical to df_to_double where
+// `ok` is set and cheaper because it carries none of the range cases: a
+// caller converts with it and falls back to the full routine (per complex
+// value) where `ok` is false.  The radix-8 and mixed-radix kernels store
+// through it (it shortens the ALU-bound store phase of a last pass: 512^3
+// complex128, 1.17 -> 1.06 ms); their loads use the branch-free
+// df_from_double, which measured faster there than a fast path with a
+// fallback.
+//
+// float-float -> double where the renormalised high word h has a biased
+// exponent in 52..254 (|h| >= 2^-75: the scale 2^(52 - e_h) is a float)
+// and a non-zero mantissa field (the sum cannot leave h's binade
+// downwards), and for zeros.  The sign of h is folded into the scale, so
+// that the rounded count L is already directed.
+__device__ __forceinline__ double df_to_double_fast(df v, bool& ok) {
+  const float hi = __fadd_rn(v.hi, v.lo);
+  const float lo = __fsub_rn(v.lo, __fsub_rn(hi, v.hi));
+  const unsigned uh = __float_as_uint(hi);
+  const unsigned sign = uh & 0x80000000u;
+  const unsigned ehb = uh & 0x7F800000u;
+  const unsigned sb = (306u << 23) - ehb;  // 2^(52 - e_hi)
+  const int L = __float2int_rn(__fmul_rn(lo, __uint_as_float(sb | sign)));
+  const unsigned dh = sign | (((uh & 0x7FFFFFFFu) >> 3) + (896u << 20));
+  unsigned long long P = (((unsigned long long)dh << 32) | (uh << 29)) + (unsigned long long)(long long)L;
+  const bool zero = ehb == 0u;
+  if (zero) P = (unsigned long long)sign << 32;
+  ok = ((ehb - (52u << 23)) <= (202u << 23) && (uh & 0x7FFFFFu) != 0u) || zero;
+  return __longlong_as_double((long long)P);
+}
+
+// The store conversion as the kernels use it: the fast path, and the full
+// routine for a value (or pair) outside it.
+__device__ __forceinline__ double df_to_double_sel(df v) {
+  bool ok;
+  const double r = df_to_double_fast(v, ok);
+  return ok ? r : df_to_double(v);
+}
+__device__ __forceinline__ void df_pair_to_double(df a, df b, double& ra, double& rb) {
+  bool oa, ob;
+  ra = df_to_double_fast(a, oa);
+  rb = df_to_double_fast(b, ob);
+  if (!(oa && ob)) {
+    ra = df_to_double(a);
+    rb = df_to_double(b);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Policies
 // ---------------------------------------------------------------------------

@@ -95,9 +95,8 @@ __device__ __forceinline__ void batch_fast_n(const BatchPass& bp, long long tile
   }
 }
 
-template <bool DOUBLE>
-__device__ __forceinline__ void batch_fast(const BatchPass& bp, long long tile, unsigned char* sm) {
-  typedef typename std::conditional<DOUBLE, fast::FDD, fast::F32>::type P;
+template <class P>
+__device__ __forceinline__ void batch_fast_p(const BatchPass& bp, long long tile, unsigned char* sm) {
   switch (bp.fastN) {
     case 16: batch_fast_n<P, 16>(bp, tile, sm); break;
     case 32: batch_fast_n<P, 32>(bp, tile, sm); break;
@@ -105,6 +104,20 @@ __device__ __forceinline__ void batch_fast(const BatchPass& bp, long long tile, 
     case 128: batch_fast_n<P, 128>(bp, tile, sm); break;
     case 256: batch_fast_n<P, 256>(bp, tile, sm); break;
     default: batch_fast_n<P, 512>(bp, tile, sm); break;
+  }
+}
+
+// double batches: the arithmetic of the pass's plan (TwoSum or
+// block-quantised float-float radix-8 stages, PassParams::quant)
+template <bool DOUBLE>
+__device__ __forceinline__ void batch_fast(const BatchPass& bp, long long tile, unsigned char* sm) {
+  if constexpr (DOUBLE) {
+    if (bp.p.quant)
+      batch_fast_p<fast::FQ>(bp, tile, sm);
+    else
+      batch_fast_p<fast::FDD>(bp, tile, sm);
+  } else {
+    batch_fast_p<fast::F32>(bp, tile, sm);
   }
 }
 

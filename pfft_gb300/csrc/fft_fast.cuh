@@ -190,7 +190,9 @@ struct FDD {
     return from_df(df_from_double(v.x), df_from_double(v.y));
   }
   static __device__ __forceinline__ void st(G* p, C v) {
-    *p = make_double2(df_to_double(re_df(v)), df_to_double(im_df(v)));
+    double re, im;
+    df_pair_to_double(re_df(v), im_df(v), re, im);
+    *p = make_double2(re, im);
   }
   static __device__ __forceinline__ C lds(const S& s) { return {make_float2(s.x, s.y), make_float2(s.z, s.w)}; }
   static __device__ __forceinline__ S sts(C v) { return make_float4(v.h.x, v.h.y, v.l.x, v.l.y); }
@@ -490,7 +492,7 @@ __device__ __forceinline__ void rstore<F32>(void* dst, long long i, F32::C v) {
 }
 template <>
 __device__ __forceinline__ void rstore<FDD>(void* dst, long long i, FDD::C v) {
-  ((double*)dst)[i] = df_to_double(FDD::re_df(v));
+  ((double*)dst)[i] = df_to_double_sel(FDD::re_df(v));
 }
 template <class P>
 __device__ __forceinline__ typename P::C czero();

@@ -95,7 +95,20 @@ int launch_pass(const PassParams& p, int arith, cudaStream_t stream) {
 namespace {
 __global__ void k_df_roundtrip(const double* in, double* out, long long n) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) out[i] = pg::df_to_double(pg::df_from_double(in[i]));
+  if (i < n) out[i] = pg::df_to_double_sel(pg::df_from_double(in[i]));
+}
+// pairs (hi, lo): the fast float-float -> double conversion against the full
+// one.  Counts: [0] values the fast path took, [1] its results that differ.
+__global__ void k_df_fast(const float2* in, long long n, unsigned long long* counts) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  bool ok;
+  const pg::df d{in[i].x, in[i].y};
+  const double f = pg::df_to_double_fast(d, ok), g = pg::df_to_double(d);
+  if (ok) {
+    atomicAdd(counts, 1ull);
+    if (__double_as_longlong(f) != __double_as_longlong(g)) atomicAdd(counts + 1, 1ull);
+  }
 }
 }  // namespace
 
@@ -104,5 +117,13 @@ __global__ void k_df_roundtrip(const double* in, double* out, long long n) {
 extern "C" int pfft_gb300_selftest_df_roundtrip(const double* in, double* out, long long n, void* stream) {
   if (n <= 0) return 0;
   k_df_roundtrip<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(in, out, n);
+  return (int)cudaGetLastError();
+}
+
+// Test hook: agreement of the float-float -> double fast path with the full
+// routine (device arrays; counts = two zeroed device words, see k_df_fast).
+extern "C" int pfft_gb300_selftest_df_fast(const float* pairs, long long n, unsigned long long* counts, void* stream) {
+  if (n <= 0) return 0;
+  k_df_fast<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>((const float2*)pairs, n, counts);
   return (int)cudaGetLastError();
 }

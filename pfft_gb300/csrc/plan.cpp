@@ -72,7 +72,8 @@ void set_double_arith(int a) { g_double_arith = a; }
 // Arithmetic of one double-precision plan.  Native FP64 issues at about 1/64
 // of the FP32 rate on this part, so large transforms run in float-float; a
 // transform of at most DARITH_AUTO_POINTS points costs no more than a launch
-// latency in FP64 and keeps full double rounding.
+// latency in FP64 and keeps full double rounding.  (Whether the float-float
+// radix-8 stages are block-quantised is Plan::quant, set with the arithmetic.)
 int plan_double_arith(const PlanDesc& d) {
   const int m = double_arith();
   if (m == DARITH_NATIVE) return ARITH_F64;
@@ -83,8 +84,9 @@ int plan_double_arith(const PlanDesc& d) {
 }
 
 // Block-quantised float-float radix-8 stages (fft_fast.cuh, FQ) for the
-// plain power-of-two c2c passes of a float-float plan: chosen with the
-// double-arithmetic mode DARITH_DFQ.
+// plain power-of-two c2c passes of a float-float plan: the double-arithmetic
+// modes DARITH_DFQ and DARITH_AUTO (above DARITH_AUTO_POINTS); DARITH_DF
+// keeps TwoSum additions everywhere.
 static void mark_quant(const Plan* pl, PassProgram* prog) {
   for (Pass& ps : prog->passes) ps.p.quant = pl->quant;
 }
@@ -147,7 +149,7 @@ Plan* make_plan(const PlanDesc& base, void* in, void* out) {
   Plan* pl = new Plan();
   pl->d = base;
   pl->arith = base.prec == 0 ? ARITH_F32 : plan_double_arith(base);
-  pl->quant = (pl->arith == ARITH_DF && double_arith() == DARITH_DFQ) ? 1 : 0;
+  pl->quant = (pl->arith == ARITH_DF && (double_arith() == DARITH_DFQ || double_arith() == DARITH_AUTO)) ? 1 : 0;
   pl->in = in;
   pl->out = out;
   pl->inplace = (in == out) && in != nullptr;
