@@ -341,6 +341,8 @@ def main():
     ap.add_argument("--no-tune", action="store_true",
                     help="plan with PFFT_MEASURE instead of PFFT_PATIENT (by default the autotuner times every "
                          "pass's candidates at planning time, before the timed region)")
+    ap.add_argument("--batched-only", default=None, choices=["double", "float"],
+                    help="print only the batched-vs-loop measurement of that precision (profiling runs)")
     ap.add_argument("--prec", default="double", choices=["double", "float"],
                     help="double = pfft_ (complex128, the headline); float = pfftf_ (complex64)")
     args = ap.parse_args()
@@ -354,6 +356,9 @@ def main():
     import pfft_gb300 as pg
     torch.cuda.set_device(local)
     L = pg.lib()
+    if args.batched_only:
+        print(json.dumps(measure_batched(L, pg, torch, args.batched_only, tune=not args.no_tune)), flush=True)
+        return
     dev = torch.device("cuda", local)
     n = tuple(int(v) for v in args.shape.split("x")) if args.shape else (args.n, args.n, args.n)
     cnt = int(np.prod(n))

@@ -331,12 +331,14 @@ template <bool DOUBLE>
 __global__ void __launch_bounds__(BATCH_THREADS, 3) k_batch(const BatchLaunch q) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ int s_task;
+  if (threadIdx.x == 0) s_task = (int)atomicAdd(q.next, 1u);
+  __syncthreads();
   for (;;) {
-    if (threadIdx.x == 0) s_task = (int)atomicAdd(q.next, 1u);
-    __syncthreads();
     const int t = s_task;
-    __syncthreads();
     if (t >= q.ntasks) break;
+    // the next ticket is taken now, so that its round trip overlaps this tile
+    int next_t = 0;
+    if (threadIdx.x == 0) next_t = (int)atomicAdd(q.next, 1u);
     const BatchTask task = q.tasks[t];
     const BatchPass& bp = q.passes[task.pass];
     if (task.dep >= 0) {
@@ -377,9 +379,17 @@ __global__ void __launch_bounds__(BATCH_THREADS, 3) k_batch(const BatchLaunch q)
       else
         neg ? bt_gen_df_m(bp.p, tile, sm) : bt_gen_df_p(bp.p, tile, sm);
     }
-    __threadfence();
+    // publish: every thread's stores are ordered before thread 0's fence by
+    // the barrier, the fence makes them visible at device scope before the
+    // counter increment (release pattern; the waiting side loads the counter,
+    // fences, then synchronises its block)
     __syncthreads();
-    if (threadIdx.x == 0) atomicAdd(q.counters + bp.done, 1u);
+    if (threadIdx.x == 0) {
+      __threadfence();
+      atomicAdd(q.counters + bp.done, 1u);
+      s_task = next_t;
+    }
+    __syncthreads();
   }
 }
 
