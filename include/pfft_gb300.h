@@ -99,9 +99,10 @@ int pfft_gb300_selftest_df_fast(const float *pairs, long long n, unsigned long l
  *      FP32 rate on GB300)
  *   2  by size (default): native FP64 for transforms of at most 2^18 points
  *      (howmany included), mode 3 above.
- *   3  float-float whose power-of-two c2c passes on the radix-8 kernel round
- *      the high words of each radix-8 butterfly to a common grid, so that the
- *      butterfly's additions are exact without TwoSum: fewer FP32
+ *   3  float-float whose c2c passes on the radix-8 and mixed-radix kernels
+ *      (2^a, 3 * 2^a, 5 * 2^a points) round the high words of each butterfly
+ *      to a common grid, so that the butterfly's additions are exact without
+ *      TwoSum: fewer FP32
  *      operations, relative L2 error about 2e-13 per pass (bounded by a
  *      small multiple of 2^-45 per radix-8 stage, relative to the data's L2
  *      norm); other passes as in mode 0.

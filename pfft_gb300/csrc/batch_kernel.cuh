@@ -124,203 +124,58 @@ __device__ __forceinline__ void batch_fast(const BatchPass& bp, long long tile, 
 // Mixed-radix tiles (3 * 2^a and 5 * 2^a lengths), callee units
 // batch_tiles_mixed_<arith>_<family>.cu, 80 registers like the general tiles.
 #define PG_BT_MX(name) __device__ void name(const fast::FastArgs& a, long long tile, unsigned char* sm)
-PG_BT_MX(bt_mx_F32_24_rm);
-PG_BT_MX(bt_mx_F32_24_rp);
-PG_BT_MX(bt_mx_F32_24_cm);
-PG_BT_MX(bt_mx_F32_24_cp);
-PG_BT_MX(bt_mx_F32_48_rm);
-PG_BT_MX(bt_mx_F32_48_rp);
-PG_BT_MX(bt_mx_F32_48_cm);
-PG_BT_MX(bt_mx_F32_48_cp);
-PG_BT_MX(bt_mx_F32_96_rm);
-PG_BT_MX(bt_mx_F32_96_rp);
-PG_BT_MX(bt_mx_F32_96_cm);
-PG_BT_MX(bt_mx_F32_96_cp);
-PG_BT_MX(bt_mx_F32_192_rm);
-PG_BT_MX(bt_mx_F32_192_rp);
-PG_BT_MX(bt_mx_F32_192_cm);
-PG_BT_MX(bt_mx_F32_192_cp);
-PG_BT_MX(bt_mx_F32_384_rm);
-PG_BT_MX(bt_mx_F32_384_rp);
-PG_BT_MX(bt_mx_F32_384_cm);
-PG_BT_MX(bt_mx_F32_384_cp);
-PG_BT_MX(bt_mx_F32_768_rm);
-PG_BT_MX(bt_mx_F32_768_rp);
-PG_BT_MX(bt_mx_F32_768_cm);
-PG_BT_MX(bt_mx_F32_768_cp);
-PG_BT_MX(bt_mx_F32_40_rm);
-PG_BT_MX(bt_mx_F32_40_rp);
-PG_BT_MX(bt_mx_F32_40_cm);
-PG_BT_MX(bt_mx_F32_40_cp);
-PG_BT_MX(bt_mx_F32_80_rm);
-PG_BT_MX(bt_mx_F32_80_rp);
-PG_BT_MX(bt_mx_F32_80_cm);
-PG_BT_MX(bt_mx_F32_80_cp);
-PG_BT_MX(bt_mx_F32_160_rm);
-PG_BT_MX(bt_mx_F32_160_rp);
-PG_BT_MX(bt_mx_F32_160_cm);
-PG_BT_MX(bt_mx_F32_160_cp);
-PG_BT_MX(bt_mx_F32_320_rm);
-PG_BT_MX(bt_mx_F32_320_rp);
-PG_BT_MX(bt_mx_F32_320_cm);
-PG_BT_MX(bt_mx_F32_320_cp);
-PG_BT_MX(bt_mx_F32_640_rm);
-PG_BT_MX(bt_mx_F32_640_rp);
-PG_BT_MX(bt_mx_F32_640_cm);
-PG_BT_MX(bt_mx_F32_640_cp);
-PG_BT_MX(bt_mx_FDD_24_rm);
-PG_BT_MX(bt_mx_FDD_24_rp);
-PG_BT_MX(bt_mx_FDD_24_cm);
-PG_BT_MX(bt_mx_FDD_24_cp);
-PG_BT_MX(bt_mx_FDD_48_rm);
-PG_BT_MX(bt_mx_FDD_48_rp);
-PG_BT_MX(bt_mx_FDD_48_cm);
-PG_BT_MX(bt_mx_FDD_48_cp);
-PG_BT_MX(bt_mx_FDD_96_rm);
-PG_BT_MX(bt_mx_FDD_96_rp);
-PG_BT_MX(bt_mx_FDD_96_cm);
-PG_BT_MX(bt_mx_FDD_96_cp);
-PG_BT_MX(bt_mx_FDD_192_rm);
-PG_BT_MX(bt_mx_FDD_192_rp);
-PG_BT_MX(bt_mx_FDD_192_cm);
-PG_BT_MX(bt_mx_FDD_192_cp);
-PG_BT_MX(bt_mx_FDD_384_rm);
-PG_BT_MX(bt_mx_FDD_384_rp);
-PG_BT_MX(bt_mx_FDD_384_cm);
-PG_BT_MX(bt_mx_FDD_384_cp);
-PG_BT_MX(bt_mx_FDD_768_rm);
-PG_BT_MX(bt_mx_FDD_768_rp);
-PG_BT_MX(bt_mx_FDD_768_cm);
-PG_BT_MX(bt_mx_FDD_768_cp);
-PG_BT_MX(bt_mx_FDD_40_rm);
-PG_BT_MX(bt_mx_FDD_40_rp);
-PG_BT_MX(bt_mx_FDD_40_cm);
-PG_BT_MX(bt_mx_FDD_40_cp);
-PG_BT_MX(bt_mx_FDD_80_rm);
-PG_BT_MX(bt_mx_FDD_80_rp);
-PG_BT_MX(bt_mx_FDD_80_cm);
-PG_BT_MX(bt_mx_FDD_80_cp);
-PG_BT_MX(bt_mx_FDD_160_rm);
-PG_BT_MX(bt_mx_FDD_160_rp);
-PG_BT_MX(bt_mx_FDD_160_cm);
-PG_BT_MX(bt_mx_FDD_160_cp);
-PG_BT_MX(bt_mx_FDD_320_rm);
-PG_BT_MX(bt_mx_FDD_320_rp);
-PG_BT_MX(bt_mx_FDD_320_cm);
-PG_BT_MX(bt_mx_FDD_320_cp);
-PG_BT_MX(bt_mx_FDD_640_rm);
-PG_BT_MX(bt_mx_FDD_640_rp);
-PG_BT_MX(bt_mx_FDD_640_cm);
-PG_BT_MX(bt_mx_FDD_640_cp);
+// the four tiles of a length: rows / columns, forward / backward
+#define PG_BT_MX4(P, N) \
+  PG_BT_MX(bt_mx_##P##_##N##_rm); \
+  PG_BT_MX(bt_mx_##P##_##N##_rp); \
+  PG_BT_MX(bt_mx_##P##_##N##_cm); \
+  PG_BT_MX(bt_mx_##P##_##N##_cp)
+#define PG_BT_MX_ALL(P)                                                                                    \
+  PG_BT_MX4(P, 24); PG_BT_MX4(P, 48); PG_BT_MX4(P, 96); PG_BT_MX4(P, 192); PG_BT_MX4(P, 384); PG_BT_MX4(P, 768); \
+  PG_BT_MX4(P, 40); PG_BT_MX4(P, 80); PG_BT_MX4(P, 160); PG_BT_MX4(P, 320); PG_BT_MX4(P, 640)
+PG_BT_MX_ALL(F32);
+PG_BT_MX_ALL(FDD);
+PG_BT_MX_ALL(FQ);
 #define PG_BT_DEF_MX(P, N)                                                                                       \
   PG_BT_MX(bt_mx_##P##_##N##_rm) { fast::mixed_tile<fast::P, -1, N, fast::mixed_L<fast::P>(N), true, true, true>(a, tile, sm); }   \
   PG_BT_MX(bt_mx_##P##_##N##_rp) { fast::mixed_tile<fast::P, 1, N, fast::mixed_L<fast::P>(N), true, true, true>(a, tile, sm); }    \
   PG_BT_MX(bt_mx_##P##_##N##_cm) { fast::mixed_tile<fast::P, -1, N, fast::mixed_L<fast::P>(N), false, false, true>(a, tile, sm); } \
   PG_BT_MX(bt_mx_##P##_##N##_cp) { fast::mixed_tile<fast::P, 1, N, fast::mixed_L<fast::P>(N), false, false, true>(a, tile, sm); }
 
+// one of the four tiles of policy P and length N
+#define PG_BT_MX_CALL(P, N)                                                    \
+  do {                                                                         \
+    if (bp.frow)                                                               \
+      neg ? bt_mx_##P##_##N##_rm(bp.fa, tile, sm) : bt_mx_##P##_##N##_rp(bp.fa, tile, sm); \
+    else                                                                       \
+      neg ? bt_mx_##P##_##N##_cm(bp.fa, tile, sm) : bt_mx_##P##_##N##_cp(bp.fa, tile, sm); \
+  } while (0)
+// double batches: the arithmetic of the pass's plan (PassParams::quant)
+#define PG_BT_MX_CASE(N)                 \
+  case N:                                \
+    if (!DOUBLE)                         \
+      PG_BT_MX_CALL(F32, N);             \
+    else if (bp.p.quant)                 \
+      PG_BT_MX_CALL(FQ, N);              \
+    else                                 \
+      PG_BT_MX_CALL(FDD, N);             \
+    break
+
 template <bool DOUBLE>
 __device__ __forceinline__ void batch_mixed(const BatchPass& bp, long long tile, unsigned char* sm) {
   const bool neg = bp.p.sign < 0;
   switch (bp.fastN) {
-    case 24:
-      if (DOUBLE) {
-        if (bp.frow) neg ? bt_mx_FDD_24_rm(bp.fa, tile, sm) : bt_mx_FDD_24_rp(bp.fa, tile, sm);
-        else neg ? bt_mx_FDD_24_cm(bp.fa, tile, sm) : bt_mx_FDD_24_cp(bp.fa, tile, sm);
-      } else {
-        if (bp.frow) neg ? bt_mx_F32_24_rm(bp.fa, tile, sm) : bt_mx_F32_24_rp(bp.fa, tile, sm);
-        else neg ? bt_mx_F32_24_cm(bp.fa, tile, sm) : bt_mx_F32_24_cp(bp.fa, tile, sm);
-      }
-      break;
-    case 48:
-      if (DOUBLE) {
-        if (bp.frow) neg ? bt_mx_FDD_48_rm(bp.fa, tile, sm) : bt_mx_FDD_48_rp(bp.fa, tile, sm);
-        else neg ? bt_mx_FDD_48_cm(bp.fa, tile, sm) : bt_mx_FDD_48_cp(bp.fa, tile, sm);
-      } else {
-        if (bp.frow) neg ? bt_mx_F32_48_rm(bp.fa, tile, sm) : bt_mx_F32_48_rp(bp.fa, tile, sm);
-        else neg ? bt_mx_F32_48_cm(bp.fa, tile, sm) : bt_mx_F32_48_cp(bp.fa, tile, sm);
-      }
-      break;
-    case 96:
-      if (DOUBLE) {
-        if (bp.frow) neg ? bt_mx_FDD_96_rm(bp.fa, tile, sm) : bt_mx_FDD_96_rp(bp.fa, tile, sm);
-        else neg ? bt_mx_FDD_96_cm(bp.fa, tile, sm) : bt_mx_FDD_96_cp(bp.fa, tile, sm);
-      } else {
-        if (bp.frow) neg ? bt_mx_F32_96_rm(bp.fa, tile, sm) : bt_mx_F32_96_rp(bp.fa, tile, sm);
-        else neg ? bt_mx_F32_96_cm(bp.fa, tile, sm) : bt_mx_F32_96_cp(bp.fa, tile, sm);
-      }
-      break;
-    case 192:
-      if (DOUBLE) {
-        if (bp.frow) neg ? bt_mx_FDD_192_rm(bp.fa, tile, sm) : bt_mx_FDD_192_rp(bp.fa, tile, sm);
-        else neg ? bt_mx_FDD_192_cm(bp.fa, tile, sm) : bt_mx_FDD_192_cp(bp.fa, tile, sm);
-      } else {
-        if (bp.frow) neg ? bt_mx_F32_192_rm(bp.fa, tile, sm) : bt_mx_F32_192_rp(bp.fa, tile, sm);
-        else neg ? bt_mx_F32_192_cm(bp.fa, tile, sm) : bt_mx_F32_192_cp(bp.fa, tile, sm);
-      }
-      break;
-    case 384:
-      if (DOUBLE) {
-        if (bp.frow) neg ? bt_mx_FDD_384_rm(bp.fa, tile, sm) : bt_mx_FDD_384_rp(bp.fa, tile, sm);
-        else neg ? bt_mx_FDD_384_cm(bp.fa, tile, sm) : bt_mx_FDD_384_cp(bp.fa, tile, sm);
-      } else {
-        if (bp.frow) neg ? bt_mx_F32_384_rm(bp.fa, tile, sm) : bt_mx_F32_384_rp(bp.fa, tile, sm);
-        else neg ? bt_mx_F32_384_cm(bp.fa, tile, sm) : bt_mx_F32_384_cp(bp.fa, tile, sm);
-      }
-      break;
-    case 768:
-      if (DOUBLE) {
-        if (bp.frow) neg ? bt_mx_FDD_768_rm(bp.fa, tile, sm) : bt_mx_FDD_768_rp(bp.fa, tile, sm);
-        else neg ? bt_mx_FDD_768_cm(bp.fa, tile, sm) : bt_mx_FDD_768_cp(bp.fa, tile, sm);
-      } else {
-        if (bp.frow) neg ? bt_mx_F32_768_rm(bp.fa, tile, sm) : bt_mx_F32_768_rp(bp.fa, tile, sm);
-        else neg ? bt_mx_F32_768_cm(bp.fa, tile, sm) : bt_mx_F32_768_cp(bp.fa, tile, sm);
-      }
-      break;
-    case 40:
-      if (DOUBLE) {
-        if (bp.frow) neg ? bt_mx_FDD_40_rm(bp.fa, tile, sm) : bt_mx_FDD_40_rp(bp.fa, tile, sm);
-        else neg ? bt_mx_FDD_40_cm(bp.fa, tile, sm) : bt_mx_FDD_40_cp(bp.fa, tile, sm);
-      } else {
-        if (bp.frow) neg ? bt_mx_F32_40_rm(bp.fa, tile, sm) : bt_mx_F32_40_rp(bp.fa, tile, sm);
-        else neg ? bt_mx_F32_40_cm(bp.fa, tile, sm) : bt_mx_F32_40_cp(bp.fa, tile, sm);
-      }
-      break;
-    case 80:
-      if (DOUBLE) {
-        if (bp.frow) neg ? bt_mx_FDD_80_rm(bp.fa, tile, sm) : bt_mx_FDD_80_rp(bp.fa, tile, sm);
-        else neg ? bt_mx_FDD_80_cm(bp.fa, tile, sm) : bt_mx_FDD_80_cp(bp.fa, tile, sm);
-      } else {
-        if (bp.frow) neg ? bt_mx_F32_80_rm(bp.fa, tile, sm) : bt_mx_F32_80_rp(bp.fa, tile, sm);
-        else neg ? bt_mx_F32_80_cm(bp.fa, tile, sm) : bt_mx_F32_80_cp(bp.fa, tile, sm);
-      }
-      break;
-    case 160:
-      if (DOUBLE) {
-        if (bp.frow) neg ? bt_mx_FDD_160_rm(bp.fa, tile, sm) : bt_mx_FDD_160_rp(bp.fa, tile, sm);
-        else neg ? bt_mx_FDD_160_cm(bp.fa, tile, sm) : bt_mx_FDD_160_cp(bp.fa, tile, sm);
-      } else {
-        if (bp.frow) neg ? bt_mx_F32_160_rm(bp.fa, tile, sm) : bt_mx_F32_160_rp(bp.fa, tile, sm);
-        else neg ? bt_mx_F32_160_cm(bp.fa, tile, sm) : bt_mx_F32_160_cp(bp.fa, tile, sm);
-      }
-      break;
-    case 320:
-      if (DOUBLE) {
-        if (bp.frow) neg ? bt_mx_FDD_320_rm(bp.fa, tile, sm) : bt_mx_FDD_320_rp(bp.fa, tile, sm);
-        else neg ? bt_mx_FDD_320_cm(bp.fa, tile, sm) : bt_mx_FDD_320_cp(bp.fa, tile, sm);
-      } else {
-        if (bp.frow) neg ? bt_mx_F32_320_rm(bp.fa, tile, sm) : bt_mx_F32_320_rp(bp.fa, tile, sm);
-        else neg ? bt_mx_F32_320_cm(bp.fa, tile, sm) : bt_mx_F32_320_cp(bp.fa, tile, sm);
-      }
-      break;
-    case 640:
-      if (DOUBLE) {
-        if (bp.frow) neg ? bt_mx_FDD_640_rm(bp.fa, tile, sm) : bt_mx_FDD_640_rp(bp.fa, tile, sm);
-        else neg ? bt_mx_FDD_640_cm(bp.fa, tile, sm) : bt_mx_FDD_640_cp(bp.fa, tile, sm);
-      } else {
-        if (bp.frow) neg ? bt_mx_F32_640_rm(bp.fa, tile, sm) : bt_mx_F32_640_rp(bp.fa, tile, sm);
-        else neg ? bt_mx_F32_640_cm(bp.fa, tile, sm) : bt_mx_F32_640_cp(bp.fa, tile, sm);
-      }
-      break;
+    PG_BT_MX_CASE(24);
+    PG_BT_MX_CASE(48);
+    PG_BT_MX_CASE(96);
+    PG_BT_MX_CASE(192);
+    PG_BT_MX_CASE(384);
+    PG_BT_MX_CASE(768);
+    PG_BT_MX_CASE(40);
+    PG_BT_MX_CASE(80);
+    PG_BT_MX_CASE(160);
+    PG_BT_MX_CASE(320);
+    PG_BT_MX_CASE(640);
   }
 }
 

@@ -243,6 +243,11 @@ int launch_fast_pass(const PassParams& p, int arith, cudaStream_t stream) {
                                  : launch_mixed_five<F32, -1>(N, a, row_in, row_out, stream))
                         : (three ? launch_mixed_three<F32, 1>(N, a, row_in, row_out, stream)
                                  : launch_mixed_five<F32, 1>(N, a, row_in, row_out, stream));
+    if (p.quant)  // block-quantised float-float butterflies
+      return sign < 0 ? (three ? launch_mixed_three<FQ, -1>(N, a, row_in, row_out, stream)
+                                 : launch_mixed_five<FQ, -1>(N, a, row_in, row_out, stream))
+                        : (three ? launch_mixed_three<FQ, 1>(N, a, row_in, row_out, stream)
+                                 : launch_mixed_five<FQ, 1>(N, a, row_in, row_out, stream));
     return sign < 0 ? (three ? launch_mixed_three<FDD, -1>(N, a, row_in, row_out, stream)
                                : launch_mixed_five<FDD, -1>(N, a, row_in, row_out, stream))
                       : (three ? launch_mixed_three<FDD, 1>(N, a, row_in, row_out, stream)

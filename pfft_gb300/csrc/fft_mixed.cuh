@@ -84,12 +84,109 @@ __device__ __forceinline__ void bf5(typename P::C* v) {
   v[3] = P::sub(m2, n2);
 }
 
+// ---- block-quantised butterflies (FQ, fft_fast.cuh) ---------------------------------
+// The R inputs of a butterfly are rounded to a grid q = 2^(T-24) common to the
+// butterfly, T = e - 126 + H for the biased exponent e of the largest high
+// word m (m < 2^(e-126)), with 2^H above the radix's bound on every partial
+// sum: 2m (radix 2), 4m (radix 4), (2 + sqrt 3) m (radix 3),
+// (1 + 2|C1| + 2|C2|) m + 2 (S1 + S2) m = 6.3 m (radix 5, with C, S the
+// cosines and sines of 2 pi / 5 and 4 pi / 5), and H >= 2 in any case: the
+// rounding x + c1 - c1 (c1 = 0.75 * 2^T) stays in c1's binade, so on the grid,
+// only for |x| < 2^(T-2).  H = 2 for radices 2, 3 and 4, 3 for radix 5.  Sums of grid points
+// below 2^T are exact; the products with the radix's constants (at most
+// sqrt 3 m for radix 3, 1.9 m for radix 5: below 2^(T-1)) are put back on the
+// grid one binade up (ulp 2q), their remainders moved to the low words.
+template <int R>
+__host__ __device__ constexpr int fq_head() {
+  return R == 5 ? 3 : 2;
+}
+template <int R>
+__device__ __forceinline__ void fq_grid(const FDD::C* v, float2& c1, float2& c2) {
+  constexpr unsigned H = (unsigned)fq_head<R>();
+  float m = fmaxf(fabsf(v[0].h.x), fabsf(v[0].h.y));
+#pragma unroll
+  for (int r = 1; r < R; r++) m = fmaxf(m, fmaxf(fabsf(v[r].h.x), fabsf(v[r].h.y)));
+  const unsigned eb = min(__float_as_uint(m) & 0x7F800000u, (253u - H) << 23);  // c2 stays finite
+  const float a = __uint_as_float(eb + (H << 23) + 0x400000u);         // 1.5 * 2^(T-1): ulp q
+  const float b = __uint_as_float(eb + ((H + 1u) << 23) + 0x400000u);  // 1.5 * 2^T: ulp 2q
+  c1 = make_float2(a, a);
+  c2 = make_float2(b, b);
+}
+// k * a for a float-float constant k (exact product of the high words plus
+// its error terms), the high word back on the grid of c
+__device__ __forceinline__ FDD::C fq_mulc(FDD::C a, DD k, float2 c) {
+  const float2 kh = make_float2(k.hi, k.hi), kl = make_float2(k.lo, k.lo);
+  const float2 p = mul2(a.h, kh);
+  float2 e = fma2(a.h, kh, neg2(p));
+  e = fma2(a.h, kl, e);
+  e = fma2(a.l, kh, e);
+  const float2 pq = sub2(add2(p, c), c);
+  return {pq, add2(e, sub2(p, pq))};
+}
+template <int SIGN>
+__device__ __forceinline__ void fq_bf3(FDD::C* v) {
+  constexpr double S3 = 0.86602540378443864676372317075294;
+  float2 c1, c2;
+  fq_grid<3>(v, c1, c2);
+#pragma unroll
+  for (int r = 0; r < 3; r++) v[r] = fq_round(v[r], c1);
+  const FDD::C t = fq_add(v[1], v[2]), u = fq_sub(v[1], v[2]), a0 = v[0];
+  v[0] = fq_add(a0, t);
+  const FDD::C m = fq_sub(a0, fq_mulc(t, PG_KC(FDD, 0.5), c2));
+  const FDD::C su = msi<FDD, SIGN>(fq_mulc(u, PG_KC(FDD, S3), c2));
+  v[1] = fq_add(m, su);
+  v[2] = fq_sub(m, su);
+}
+template <int SIGN>
+__device__ __forceinline__ void fq_bf5(FDD::C* v) {
+  constexpr double C1 = 0.30901699437494742410229341718282;
+  constexpr double C2 = -0.80901699437494742410229341718282;
+  constexpr double S1 = 0.95105651629515357211643933337938;
+  constexpr double S2 = 0.58778525229247312916870595463907;
+  float2 c1, c2;
+  fq_grid<5>(v, c1, c2);
+#pragma unroll
+  for (int r = 0; r < 5; r++) v[r] = fq_round(v[r], c1);
+  const FDD::C a0 = v[0];
+  const FDD::C t1 = fq_add(v[1], v[4]), t2 = fq_add(v[2], v[3]);
+  const FDD::C u1 = fq_sub(v[1], v[4]), u2 = fq_sub(v[2], v[3]);
+  v[0] = fq_add(a0, fq_add(t1, t2));
+  const FDD::C m1 = fq_add(a0, fq_add(fq_mulc(t1, PG_KC(FDD, C1), c2), fq_mulc(t2, PG_KC(FDD, C2), c2)));
+  const FDD::C m2 = fq_add(a0, fq_add(fq_mulc(t1, PG_KC(FDD, C2), c2), fq_mulc(t2, PG_KC(FDD, C1), c2)));
+  const FDD::C n1 =
+      msi<FDD, SIGN>(fq_add(fq_mulc(u1, PG_KC(FDD, S1), c2), fq_mulc(u2, PG_KC(FDD, S2), c2)));
+  const FDD::C n2 =
+      msi<FDD, SIGN>(fq_sub(fq_mulc(u1, PG_KC(FDD, S2), c2), fq_mulc(u2, PG_KC(FDD, S1), c2)));
+  v[1] = fq_add(m1, n1);
+  v[4] = fq_sub(m1, n1);
+  v[2] = fq_add(m2, n2);
+  v[3] = fq_sub(m2, n2);
+}
+
 template <class P, int SIGN, int R>
 __device__ __forceinline__ void bfR(typename P::C* v) {
-  if constexpr (R == 2) bf2<P, SIGN>(v);
-  if constexpr (R == 3) bf3<P, SIGN>(v);
-  if constexpr (R == 4) bf4<P, SIGN>(v[0], v[1], v[2], v[3]);
-  if constexpr (R == 5) bf5<P, SIGN>(v);
+  if constexpr (std::is_same<P, FQ>::value) {
+    if constexpr (R == 2 || R == 4) {
+      float2 c1, c2;
+      fq_grid<R>(v, c1, c2);
+#pragma unroll
+      for (int r = 0; r < R; r++) v[r] = fq_round(v[r], c1);
+      if constexpr (R == 2) {
+        const FDD::C a = v[0], b = v[1];
+        v[0] = fq_add(a, b);
+        v[1] = fq_sub(a, b);
+      } else {
+        fq_bf4<SIGN>(v[0], v[1], v[2], v[3]);
+      }
+    }
+    if constexpr (R == 3) fq_bf3<SIGN>(v);
+    if constexpr (R == 5) fq_bf5<SIGN>(v);
+  } else {
+    if constexpr (R == 2) bf2<P, SIGN>(v);
+    if constexpr (R == 3) bf3<P, SIGN>(v);
+    if constexpr (R == 4) bf4<P, SIGN>(v[0], v[1], v[2], v[3]);
+    if constexpr (R == 5) bf5<P, SIGN>(v);
+  }
 }
 
 template <class P>

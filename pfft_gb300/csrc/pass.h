@@ -99,9 +99,9 @@ struct PassParams {
   int fastL;    // radix-8 kernel lines per CTA (0: default for the length)
   int staged;   // staged variant of the radix-8 kernel (plain c2c passes): 0 default
                 // (float column passes), 1 on where the layout allows, 2 off
-  int quant;    // double API, plain power-of-two c2c passes of the radix-8 kernel:
-                // float-float with block-quantised high words (1) instead of TwoSum
-                // additions (0)
+  int quant;    // double API, plain c2c passes of the radix-8 and mixed-radix
+                // kernels: float-float with block-quantised high words (1) instead
+                // of TwoSum additions (0)
 };
 
 // Launch one pass on `stream`.  Returns a cudaError_t value.

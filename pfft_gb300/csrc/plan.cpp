@@ -83,8 +83,8 @@ int plan_double_arith(const PlanDesc& d) {
   return pts <= (double)DARITH_AUTO_POINTS ? ARITH_F64 : ARITH_DF;
 }
 
-// Block-quantised float-float radix-8 stages (fft_fast.cuh, FQ) for the
-// plain power-of-two c2c passes of a float-float plan: the double-arithmetic
+// Block-quantised float-float butterflies (fft_fast.cuh / fft_mixed.cuh, FQ)
+// for the plain c2c passes of a float-float plan: the double-arithmetic
 // modes DARITH_DFQ and DARITH_AUTO (above DARITH_AUTO_POINTS); DARITH_DF
 // keeps TwoSum additions everywhere.
 static void mark_quant(const Plan* pl, PassProgram* prog) {

@@ -38,7 +38,7 @@ CASES = [
 
 
 @pytest.mark.parametrize("req", CASES, ids=lambda r: "%s-%s-%x" % (r.kind, "x".join(map(str, r.n)), r.flags))
-@pytest.mark.parametrize("prec,tol", [("double", 1e-12), ("double-df", 1e-12), ("float", 2e-6)])
+@pytest.mark.parametrize("prec,tol", [("double", 1e-12), ("double-df", 1e-12), ("double-dfq", 1e-12), ("float", 2e-6)])
 def test_dot_product_identity(cuda, pfft_lib, req, prec, tol):
     rng = np.random.default_rng(5)
     x = _mask_in_padding(req, random_input(req, rng))
@@ -66,7 +66,7 @@ def _weights_c2r_input(n_last_logical, half):
     return w
 
 
-@pytest.mark.parametrize("prec", ["double", "double-df"])
+@pytest.mark.parametrize("prec", ["double", "double-df", "double-dfq"])
 def test_r2c_adjoint_matches_reference_gradient(cuda, pfft_lib, prec):
     """Adjoint of an oversampled r2c = the reference's c2r plan (n -> ni)
     applied to the Hermitian-weighted half spectrum, then truncation."""

@@ -39,7 +39,7 @@ def make_plans(torch, prec, count, seed, flags=0):
     return pre, plans, arrays
 
 
-@pytest.mark.parametrize("prec,tol", [("double", 1e-12), ("double-df", 1e-12), ("float", 2e-6)])
+@pytest.mark.parametrize("prec,tol", [("double", 1e-12), ("double-df", 1e-12), ("double-dfq", 1e-12), ("float", 2e-6)])
 def test_batch_matches_oracle(cuda, pfft_lib, prec, tol):
     torch = cuda
     L = pg.lib()

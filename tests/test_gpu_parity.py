@@ -175,11 +175,14 @@ def test_double_arith_modes(cuda, pfft_lib):
 
 
 @pytest.mark.parametrize("n,flags", [((16, 512, 8), 0), ((512, 4, 64), TO), ((8, 16, 4096), 0), ((4, 1024, 8), TI),
-                                     ((128, 32, 256), 0), ((2048, 8, 16), TO)])
+                                     ((128, 32, 256), 0), ((2048, 8, 16), TO), ((96, 8, 768), 0), ((40, 320, 24), TO),
+                                     ((8, 640, 48), TI)])
 @pytest.mark.parametrize("sign", [-1, 1])
 def test_block_quantised_error_level(cuda, pfft_lib, n, flags, sign):
-    """The block-quantised float-float radix-8 stages ("double-dfq") stay
-    within a few times 1e-13 relative L2 per pass on uniform and normal data
+    """The block-quantised float-float butterflies ("double-dfq": radix-8
+    stages, and the radix-2/3/4/5 stages of the mixed-radix kernel on
+    3 * 2^a and 5 * 2^a lines) stay within a few times 1e-13 relative L2 per
+    transform on uniform and normal data
     and on data spanning 2^-30..2^30 in magnitude (the error is relative to
     each butterfly's largest component), against about 1e-14 for TwoSum
     float-float on the same lines."""

@@ -26,6 +26,7 @@ def pass_choices(L, pre, plan):
 
 @pytest.mark.parametrize("prec,kind,n,flags", [
     ("double-df", "c2c", (64, 96, 512), pg.PFFT_PATIENT),
+    ("double-dfq", "c2c", (32, 64, 512), pg.PFFT_PATIENT | pg.PFFT_TRANSPOSED_OUT),
     ("float", "c2c", (48, 1024, 40), pg.PFFT_TUNE | pg.PFFT_TRANSPOSED_OUT),
     ("double", "r2c", (30, 28, 64), pg.PFFT_EXHAUSTIVE),
 ])
