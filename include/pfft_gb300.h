@@ -32,13 +32,22 @@ void pfftf_execute_adjoint_arrays(const pfftf_plan plan, void *gout, void *gin);
  * stream).  sync=1 (default) makes pfft_execute return after the work is done,
  * like the reference; sync=0 leaves it queued on the stream.  graph=1 replays
  * the pass launches from a captured CUDA graph (re-captured when the arrays
- * change). All return 0 on success, -1 for a NULL plan. */
+ * change).  pipeline=1 (default) overlaps, for out-of-place executes on host
+ * arrays, the host-to-device copy of the input with the leading passes and
+ * the device-to-host copy of the output with the last pass, where the pass
+ * layout allows it; pipeline=0 stages whole arrays.  All return 0 on
+ * success, -1 for a NULL plan. */
 int pfft_gb300_set_stream(pfft_plan plan, void *stream);
 int pfftf_gb300_set_stream(pfftf_plan plan, void *stream);
 int pfft_gb300_set_sync(pfft_plan plan, int sync);
 int pfftf_gb300_set_sync(pfftf_plan plan, int sync);
 int pfft_gb300_set_graph(pfft_plan plan, int graph);
 int pfftf_gb300_set_graph(pfftf_plan plan, int graph);
+int pfft_gb300_set_pipeline(pfft_plan plan, int pipeline);
+int pfftf_gb300_set_pipeline(pfftf_plan plan, int pipeline);
+/* Executes (both precisions) that went through the host-array pipeline so far
+ * in this process. */
+long long pfft_gb300_pipelined_executes(void);
 
 /* Introspection: number of passes, algorithmic bytes of one execute (sum over
  * passes of elements read + written), and plan-owned workspace bytes. */

@@ -151,7 +151,7 @@ def _declare(L):
         for nm in ("gb300_set_stream",):
             f(nm).restype = ctypes.c_int
             f(nm).argtypes = [c_void_p, c_void_p]
-        for nm in ("gb300_set_sync", "gb300_set_graph"):
+        for nm in ("gb300_set_sync", "gb300_set_graph", "gb300_set_pipeline"):
             f(nm).restype = ctypes.c_int
             f(nm).argtypes = [c_void_p, ctypes.c_int]
         f("gb300_plan_info").restype = ctypes.c_int
@@ -200,6 +200,7 @@ def _declare(L):
     L.pfft_gb300_set_staged.argtypes = [ctypes.c_int]
     L.pfft_gb300_get_staged.restype = ctypes.c_int
     L.pfft_gb300_staged_launches.restype = ctypes.c_longlong
+    L.pfft_gb300_pipelined_executes.restype = ctypes.c_longlong
     L.pfft_gb300_staged_status.restype = ctypes.c_int
 
 

@@ -356,6 +356,11 @@ void do_execute(Plan* pl, void* in, void* out) {
     plan->p->use_graph = on != 0;                                                                         \
     return 0;                                                                                             \
   }                                                                                                       \
+  int PX##gb300_set_pipeline(PX##plan plan, int on) {                                                     \
+    if (!plan) return -1;                                                                                 \
+    plan->p->pipeline = on != 0;                                                                          \
+    return 0;                                                                                             \
+  }                                                                                                       \
   int PX##gb300_plan_info(const PX##plan plan, int* npasses, double* bytes, size_t* ws_bytes) {           \
     if (!plan) return -1;                                                                                 \
     if (npasses) *npasses = (int)plan->p->fwd.passes.size();                                              \
@@ -409,6 +414,7 @@ extern "C" {
 int pfft_gb300_last_error(void) { return last_error_code(); }
 const char* pfft_gb300_last_error_string(void) { return last_error_string(); }
 void pfft_gb300_clear_error(void) { clear_error(); }
+long long pfft_gb300_pipelined_executes(void) { return pipelined_executes(); }
 void pfft_gb300_set_kernel_path(int path) { set_kernel_path(path ? 1 : 0); }
 int pfft_gb300_get_kernel_path(void) { return kernel_path(); }
 void pfft_gb300_set_staged(int mode) { set_staged_mode(mode); }

@@ -137,6 +137,8 @@ struct TimerData {
   double itwiddle = 0, otwiddle = 0;
 };
 
+constexpr int PIPE_CHUNKS = 8;  // slabs of the host-array pipeline
+
 struct Plan {
   PlanDesc d;
   int arith = ARITH_DF;
@@ -160,6 +162,11 @@ struct Plan {
   int graph_dir = 0;
   TimerData timer;
   cudaEvent_t ev[2] = {nullptr, nullptr};
+  // host-array pipeline (plan.cpp): copy streams and chunk events, made on first use
+  cudaStream_t pipe_s[2] = {nullptr, nullptr};
+  cudaEvent_t pipe_ev[2][PIPE_CHUNKS] = {};
+  cudaEvent_t pipe_done = nullptr;
+  bool pipeline = true;  // pipelined staging of host arrays where the program allows it
   // optional per-pass timing with CUDA events on the plan stream
   bool time_passes = false;
   std::vector<cudaEvent_t> pev;
@@ -195,5 +202,6 @@ constexpr long long DARITH_AUTO_POINTS = 1LL << 18;
 int double_arith();
 void set_double_arith(int a);
 int plan_double_arith(const PlanDesc& d);
+long long pipelined_executes();  // executes through the host-array pipeline (plan.cpp)
 
 }  // namespace pg

@@ -1,4 +1,5 @@
 // Plan objects: creation, execution (device or host arrays), destruction.
+#include <atomic>
 #include <stdarg.h>
 #include <stdio.h>
 #include <string.h>
@@ -194,6 +195,12 @@ void destroy_plan(Plan* pl) {
   for (int k = 0; k < 2; k++)
     if (pl->ev[k]) cudaEventDestroy(pl->ev[k]);
   for (auto e : pl->pev) cudaEventDestroy(e);
+  for (int k = 0; k < 2; k++) {
+    if (pl->pipe_s[k]) cudaStreamDestroy(pl->pipe_s[k]);
+    for (int c = 0; c < PIPE_CHUNKS; c++)
+      if (pl->pipe_ev[k][c]) cudaEventDestroy(pl->pipe_ev[k][c]);
+  }
+  if (pl->pipe_done) cudaEventDestroy(pl->pipe_done);
   delete pl;
 }
 
@@ -222,6 +229,175 @@ static size_t layout_bytes(const Layout& L, int arith) {
   return (size_t)L.span * e;
 }
 
+// ---- host-array pipeline ------------------------------------------------------
+// Out-of-place executes on host arrays stage both arrays through device
+// buffers.  When the leading passes are c2c passes whose slowest batch
+// dimension cuts the data into PIPE_CHUNKS slabs that no line crosses (and
+// consecutive passes agree on the slab size), the input is copied slab by
+// slab on a copy stream and those passes run on each slab as it arrives; when
+// the last pass is a c2c pass with one dense batch dimension (lines at a
+// stride of at least the batch extent), it runs in PIPE_CHUNKS column chunks,
+// each copied back to the host as a pitched 2-D copy on a second copy stream
+// while the next chunk is computed.  Other programs stage whole arrays.
+
+static int pass_esz(const PassParams& p, int arith, bool in) {
+  const bool c = in ? (p.mode == MODE_C2C || p.mode == MODE_C2R) : (p.mode == MODE_C2C || p.mode == MODE_R2C);
+  return c ? (arith == ARITH_F32 ? 8 : 16) : (arith == ARITH_F32 ? 4 : 8);
+}
+
+// Bytes of one of C slabs of a c2c pass's input (side 0) or output (side 1)
+// along its slowest batch dimension, or 0 when that does not cut the array
+// into slabs (the lines of one slab would reach into the next).
+static long long slab_bytes(const PassParams& p, int arith, int side, int C) {
+  if (p.mode != MODE_C2C || p.nb < 1 || p.nst == 0) return 0;
+  const int b = p.nb - 1;
+  if (p.bext[b] % C) return 0;
+  const long long* bs = side ? p.bsO : p.bsI;
+  const long long sa = side ? p.sOa : p.sIa;
+  const long long n = side ? p.No : p.Ni;
+  if (sa <= 0 || bs[b] <= 0) return 0;
+  long long inner = (n - 1) * sa + 1;
+  for (int q = 0; q < b; q++) {
+    if (bs[q] <= 0) return 0;
+    inner += (p.bext[q] - 1) * bs[q];
+  }
+  if (inner > bs[b]) return 0;
+  return (p.bext[b] / C) * bs[b] * pass_esz(p, arith, side == 0);
+}
+
+// the lines of chunk k of C along the slowest batch dimension
+static PassParams chunk_of(const PassParams& p, int arith, int k, int C) {
+  PassParams q = p;
+  const int b = p.nb - 1;
+  const long long w = p.bext[b] / C, a = (long long)k * w;
+  q.bext[b] = w;
+  q.nlines = p.nlines / C;
+  q.src = (const char*)p.src + a * p.bsI[b] * pass_esz(p, arith, true);
+  q.dst = (char*)p.dst + a * p.bsO[b] * pass_esz(p, arith, false);
+  q.bshI[b].start += (int)a;
+  q.bshO[b].start += (int)a;
+  return q;
+}
+
+static int launch_prog_pass(Plan* pl, const Pass& ps, PassParams p, cudaStream_t s) {
+  cudaError_t e;
+  p.tw = twiddle_table(p.M, pl->arith, &e);
+  if (!p.tw) return (int)e;
+  return launch_pass(p, pl->arith, s);
+}
+
+static std::atomic<long long> g_pipelined{0};
+long long pipelined_executes() { return g_pipelined.load(); }
+
+// 1: executed through the pipeline, 0: not applicable (nothing done), -1: error (reported)
+static int run_pipelined(Plan* pl, const PassProgram& prog, void* in, void* out, cudaStream_t s, size_t bin,
+                         size_t bout) {
+  const int C = PIPE_CHUNKS;
+  const int P = (int)prog.passes.size();
+  if (P < 2 || pl->inplace) return 0;
+  // leading slab passes
+  const long long s0 = slab_bytes(prog.passes[0].p, pl->arith, 0, C);
+  if (s0 < (8LL << 20) || prog.passes[0].src != BUF_IN) return 0;
+  int lead = 0;
+  while (lead < P - 1) {
+    const PassParams& p = prog.passes[lead].p;
+    const long long so = slab_bytes(p, pl->arith, 1, C);
+    if (!so) break;
+    if (lead > 0 && slab_bytes(p, pl->arith, 0, C) != slab_bytes(prog.passes[lead - 1].p, pl->arith, 1, C)) break;
+    lead++;
+  }
+  if (lead == 0) return 0;
+  // last pass in column chunks
+  const PassParams& pz = prog.passes[P - 1].p;
+  const bool tail = pz.mode == MODE_C2C && pz.nb == 1 && pz.bsO[0] == 1 && pz.sOa >= pz.bext[0] &&
+                    pz.bext[0] % C == 0 && pz.nst > 0 && prog.passes[P - 1].dst == BUF_OUT && lead < P - 1;
+  if (!ensure_stage(pl, 0, bin) || !ensure_stage(pl, 1, bout)) return -1;
+  for (int k = 0; k < 2; k++) {
+    if (!pl->pipe_s[k] && cuda_check(cudaStreamCreateWithFlags(&pl->pipe_s[k], cudaStreamNonBlocking), "copy stream"))
+      return -1;
+    for (int c = 0; c < C; c++)
+      if (!pl->pipe_ev[k][c] &&
+          cuda_check(cudaEventCreateWithFlags(&pl->pipe_ev[k][c], cudaEventDisableTiming), "pipeline event"))
+        return -1;
+  }
+  if (!pl->pipe_done && cuda_check(cudaEventCreateWithFlags(&pl->pipe_done, cudaEventDisableTiming), "pipeline event"))
+    return -1;
+  void* bufs[4] = {pl->stage[0], pl->stage[1], pl->ws[0], pl->ws[1]};
+  cudaStream_t ci = pl->pipe_s[0], co = pl->pipe_s[1];
+  // the copy streams start after the work already queued on the plan stream
+  if (cuda_check(cudaEventRecord(pl->pipe_done, s), "pipeline event") ||
+      cuda_check(cudaStreamWaitEvent(ci, pl->pipe_done, 0), "pipeline wait"))
+    return -1;
+  for (int k = 0; k < C; k++) {
+    const size_t off = (size_t)k * (size_t)s0;
+    if (off < bin) {
+      const size_t n = std::min((size_t)s0, bin - off);
+      if (cuda_check(cudaMemcpyAsync((char*)bufs[0] + off, (const char*)in + off, n, cudaMemcpyHostToDevice, ci),
+                     "host-to-device copy"))
+        return -1;
+    }
+    if (cuda_check(cudaEventRecord(pl->pipe_ev[0][k], ci), "pipeline event")) return -1;
+  }
+  int rc = 0;
+  for (int k = 0; k < C && !rc; k++) {
+    if (cuda_check(cudaStreamWaitEvent(s, pl->pipe_ev[0][k], 0), "pipeline wait")) return -1;
+    for (int i = 0; i < lead && !rc; i++) {
+      const Pass& ps = prog.passes[i];
+      PassParams p = ps.p;
+      p.src = bufs[ps.src];
+      p.dst = bufs[ps.dst];
+      rc = launch_prog_pass(pl, ps, chunk_of(p, pl->arith, k, C), s);
+    }
+  }
+  for (int i = lead; i < (tail ? P - 1 : P) && !rc; i++) {
+    const Pass& ps = prog.passes[i];
+    PassParams p = ps.p;
+    p.src = bufs[ps.src];
+    p.dst = bufs[ps.dst];
+    rc = launch_prog_pass(pl, ps, p, s);
+  }
+  if (rc) {
+    cuda_check((cudaError_t)rc, "pass launch");
+    return -1;
+  }
+  if (tail) {
+    const Pass& ps = prog.passes[P - 1];
+    PassParams p = ps.p;
+    p.src = bufs[ps.src];
+    p.dst = bufs[ps.dst];
+    const size_t esz = (size_t)pass_esz(p, pl->arith, false);
+    const size_t w = (size_t)(p.bext[0] / C) * esz, pitch = (size_t)p.sOa * esz;
+    for (int j = 0; j < C; j++) {
+      PassParams q = p;
+      q.bext[0] = p.bext[0] / C;
+      q.nlines = p.nlines / C;
+      q.dst = (char*)p.dst + (size_t)j * w;
+      q.src = (const char*)p.src + (size_t)j * (size_t)(p.bext[0] / C) * (size_t)p.bsI[0] * pass_esz(p, pl->arith, true);
+      q.bshI[0].start += (int)(j * (p.bext[0] / C));
+      q.bshO[0].start += (int)(j * (p.bext[0] / C));
+      rc = launch_prog_pass(pl, ps, q, s);
+      if (rc) {
+        cuda_check((cudaError_t)rc, "pass launch");
+        return -1;
+      }
+      if (cuda_check(cudaEventRecord(pl->pipe_ev[1][j], s), "pipeline event") ||
+          cuda_check(cudaStreamWaitEvent(co, pl->pipe_ev[1][j], 0), "pipeline wait") ||
+          cuda_check(cudaMemcpy2DAsync((char*)out + (size_t)j * w, pitch, (const char*)bufs[1] + (size_t)j * w, pitch,
+                                       w, (size_t)p.No, cudaMemcpyDeviceToHost, co),
+                     "device-to-host copy"))
+        return -1;
+    }
+    if (cuda_check(cudaEventRecord(pl->pipe_done, co), "pipeline event") ||
+        cuda_check(cudaStreamWaitEvent(s, pl->pipe_done, 0), "pipeline wait"))
+      return -1;
+  } else {
+    if (cuda_check(cudaMemcpyAsync(out, bufs[1], bout, cudaMemcpyDeviceToHost, s), "device-to-host copy")) return -1;
+  }
+  if (cuda_check(cudaStreamSynchronize(s), "execute")) return -1;
+  g_pipelined++;
+  return 1;
+}
+
 void execute_plan(Plan* pl, void* in, void* out, bool adjoint) {
   auto t0 = std::chrono::steady_clock::now();
   if (adjoint && !pl->adj_built) {
@@ -246,6 +422,16 @@ void execute_plan(Plan* pl, void* in, void* out, bool adjoint) {
   bool din = device_accessible(in), dout = device_accessible(out);
   void* xin = in;
   void* xout = out;
+  if (!din && !dout && pl->pipeline) {
+    const int r = run_pipelined(pl, prog, in, out, s, bin, bout);
+    if (r < 0) return;
+    if (r > 0) {
+      auto t1 = std::chrono::steady_clock::now();
+      pl->timer.whole += std::chrono::duration<double>(t1 - t0).count();
+      pl->timer.iter++;
+      return;
+    }
+  }
   if (!din || !dout) {
     // host arrays: stage through device buffers (copies are stream ordered)
     if (!din) {
