@@ -74,11 +74,15 @@ int pfftf_gb300_set_pass_timing(pfftf_plan plan, int on);
 int pfft_gb300_pass_time(const pfft_plan plan, int i, double *ms_total, int *runs);
 int pfftf_gb300_pass_time(const pfftf_plan plan, int i, double *ms_total, int *runs);
 
-/* Batched execution: many plans (uneven sizes, one precision) run as one
- * persistent launch - a work queue of (plan, pass, tile) entries with
- * per-plan pass dependencies - replayed from a CUDA graph.  Each plan runs on
- * the arrays it was planned with.  batch_execute returns 0, a CUDA error, or
- * -2 if a dependency wait timed out (the kernel bounds every wait). */
+/* Batched execution: many plans (uneven sizes, one precision) run as
+ * persistent launches - work queues of (plan, pass, tile) entries with
+ * per-plan pass dependencies - replayed from one CUDA graph: plans whose
+ * passes all run on the radix-8 tile in one queue (a kernel with four CTAs
+ * per SM), the others in a second (three CTAs per SM), the two launches on
+ * forked streams.  Each plan runs on the arrays it was planned with.
+ * batch_execute returns 0, a CUDA error, or -2 if a dependency wait timed out
+ * (the kernels bound every wait).  batch_info: tasks of both queues, CTAs of
+ * both launches. */
 typedef struct pfft_gb300_batch_s *pfft_gb300_batch;
 pfft_gb300_batch pfft_gb300_batch_create(int nplans, const pfft_plan *plans);
 pfft_gb300_batch pfftf_gb300_batch_create(int nplans, const pfftf_plan *plans);

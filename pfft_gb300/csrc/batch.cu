@@ -2,8 +2,12 @@
 // host side (work queue, dependency counters, CUDA graph).  The kernel is in
 // batch_kernel.cuh.
 //
-// The launch (counter reset + kernel) is captured once into a CUDA graph and
-// replayed.
+// Plans whose passes all run on the radix-8 tile go to a second queue with
+// its own persistent kernel (no callee tiles: 64 registers, four CTAs per SM,
+// as the stand-alone radix-8 kernel); the others (mixed-radix and general
+// tiles, 80-register callees, three CTAs per SM) to the first.  The launch
+// (counter reset + both kernels, the first on a forked stream) is captured
+// once into a CUDA graph and replayed.
 #include <stdio.h>
 #include <string.h>
 #include <algorithm>
@@ -26,6 +30,12 @@ struct Batch {
   int* d_err = nullptr;
   int* h_err = nullptr;  // pinned
   int ntasks = 0, ncounters = 0, threads = BATCH_THREADS, smem = 0, grid = 1;
+  // the radix-8-only queue (plans whose passes all run on the radix-8 tile):
+  // its own persistent kernel at four CTAs per SM, tasks after the others in
+  // d_tasks, ticket word after the general queue's
+  int ntasks_r8 = 0, smem_r8 = 0, grid_r8 = 0;
+  cudaStream_t side = nullptr;  // the general queue's kernel runs here when both queues are used
+  cudaEvent_t fork = nullptr, join = nullptr;
   int fast_passes = 0;
   cudaStream_t stream = 0;
   bool use_graph = true;
@@ -33,27 +43,56 @@ struct Batch {
   double bytes = 0;
 };
 
-const void* batch_kernel(int arith) { return arith == ARITH_F32 ? batch_kernel_f32() : batch_kernel_f64(); }
 
+// Counter reset, then the two persistent kernels (general queue, radix-8
+// queue); when both queues have tasks the general one runs on a forked
+// stream so that the two launches can overlap.
 int launch_batch(Batch* b, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(b->d_counters, 0, sizeof(unsigned) * (b->ncounters + 1), s);
+  cudaError_t e = cudaMemsetAsync(b->d_counters, 0, sizeof(unsigned) * (b->ncounters + 2), s);
   if (e != cudaSuccess) return (int)e;
   e = cudaMemsetAsync(b->d_err, 0, sizeof(int), s);
   if (e != cudaSuccess) return (int)e;
   BatchLaunch q;
   q.passes = b->d_passes;
-  q.tasks = b->d_tasks;
-  q.ntasks = b->ntasks;
   q.counters = b->d_counters;
-  q.next = b->d_counters + b->ncounters;
   q.err = b->d_err;
   q.spin_limit = 20000000LL;  // ~2 s of 100 ns naps
-  return b->arith == ARITH_F32 ? batch_launch_f32(q, b->grid, b->smem, s) : batch_launch_f64(q, b->grid, b->smem, s);
+  const bool both = b->ntasks > 0 && b->ntasks_r8 > 0;
+  int rc = 0;
+  if (both) {
+    if ((e = cudaEventRecord(b->fork, s)) != cudaSuccess) return (int)e;
+    if ((e = cudaStreamWaitEvent(b->side, b->fork, 0)) != cudaSuccess) return (int)e;
+  }
+  if (b->ntasks > 0) {
+    q.tasks = b->d_tasks;
+    q.ntasks = b->ntasks;
+    q.next = b->d_counters + b->ncounters;
+    cudaStream_t sg = both ? b->side : s;
+    rc = b->arith == ARITH_F32 ? batch_launch_f32(q, b->grid, b->smem, sg, false)
+                               : batch_launch_f64(q, b->grid, b->smem, sg, false);
+    if (rc) return rc;
+  }
+  if (b->ntasks_r8 > 0) {
+    q.tasks = b->d_tasks + b->ntasks;
+    q.ntasks = b->ntasks_r8;
+    q.next = b->d_counters + b->ncounters + 1;
+    rc = b->arith == ARITH_F32 ? batch_launch_f32(q, b->grid_r8, b->smem_r8, s, true)
+                               : batch_launch_f64(q, b->grid_r8, b->smem_r8, s, true);
+    if (rc) return rc;
+  }
+  if (both) {
+    if ((e = cudaEventRecord(b->join, b->side)) != cudaSuccess) return (int)e;
+    if ((e = cudaStreamWaitEvent(s, b->join, 0)) != cudaSuccess) return (int)e;
+  }
+  return 0;
 }
 
 void free_batch(Batch* b) {
   if (!b) return;
   if (b->graph) cudaGraphExecDestroy(b->graph);
+  if (b->side) cudaStreamDestroy(b->side);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->join) cudaEventDestroy(b->join);
   cudaFree(b->d_passes);
   cudaFree(b->d_tasks);
   cudaFree(b->d_counters);
@@ -68,7 +107,7 @@ Batch* make_batch(Plan* const* plans, int n) {
   b->arith = plans[0] && plans[0]->arith == ARITH_F32 ? ARITH_F32 : ARITH_DF;
   std::vector<BatchPass> hp;
   std::vector<long long> ntiles;
-  std::vector<int> first(n), npass(n);
+  std::vector<int> first(n), npass(n), r8(n);
   int maxp = 0;
   const size_t fsz = b->arith == ARITH_F32 ? sizeof(float2) : sizeof(float4);
   for (int i = 0; i < n; i++) {
@@ -83,6 +122,8 @@ Batch* make_batch(Plan* const* plans, int n) {
     first[i] = (int)hp.size();
     npass[i] = (int)pl->fwd.passes.size();
     maxp = std::max(maxp, npass[i]);
+    bool pr8 = true;  // every pass on the radix-8 tile
+    int psmem = 0;
     for (const Pass& ps : pl->fwd.passes) {
       BatchPass bp;
       memset(&bp, 0, sizeof(bp));
@@ -116,7 +157,8 @@ Batch* make_batch(Plan* const* plans, int n) {
                            : (pl->arith == ARITH_F32 ? fast::mixed_L<fast::F32>(bp.fastN) : fast::mixed_L<fast::FDD>(bp.fastN));
         tiles = (ps.p.nlines + L - 1) / L;
         const int lsp = fsz == 8 ? bp.fastN + 16 : bp.fastN + bp.fastN / 8 + 4;  // as fast_smem_bytes
-        b->smem = std::max(b->smem, (int)(16 * L + (size_t)L * lsp * fsz));
+        psmem = std::max(psmem, (int)(16 * L + (size_t)L * lsp * fsz));
+        if (bp.mixed) pr8 = false;
         b->fast_passes++;
       } else {
         bp.fastN = 0;
@@ -131,37 +173,61 @@ Batch* make_batch(Plan* const* plans, int n) {
         }
         tiles = (bp.p.nlines + bp.p.L - 1) / bp.p.L;
         bp.small = pass_is_small(bp.p) ? 1 : 0;
-        b->smem = std::max(b->smem, bp.p.smem_bytes);
+        psmem = std::max(psmem, bp.p.smem_bytes);
+        pr8 = false;
       }
       b->bytes += ps.bytes;
       hp.push_back(bp);
       ntiles.push_back(tiles);
     }
+    r8[i] = pr8 ? 1 : 0;
+    if (pr8)
+      b->smem_r8 = std::max(b->smem_r8, psmem);
+    else
+      b->smem = std::max(b->smem, psmem);
   }
   b->ncounters = (int)hp.size();
-  std::vector<BatchTask> tasks;
+  // two queues, each ordered by pass level (a task's dependency is the
+  // previous pass of its plan, in the same queue)
+  std::vector<BatchTask> tasks, tasks_r8;
   for (int lvl = 0; lvl < maxp; lvl++)
     for (int i = 0; i < n; i++) {
       if (lvl >= npass[i]) continue;
       int pi = first[i] + lvl;
       int dep = lvl > 0 ? pi - 1 : -1;
       int need = dep >= 0 ? (int)ntiles[dep] : 0;
-      for (long long t = 0; t < ntiles[pi]; t++) tasks.push_back({pi, (int)t, dep, need});
+      std::vector<BatchTask>& q = r8[i] ? tasks_r8 : tasks;
+      for (long long t = 0; t < ntiles[pi]; t++) q.push_back({pi, (int)t, dep, need});
     }
   b->ntasks = (int)tasks.size();
-  const void* kfn = batch_kernel(b->arith);
-  if (cuda_check(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, b->smem), "batch attribute")) {
+  b->ntasks_r8 = (int)tasks_r8.size();
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  for (int k = 0; k < 2; k++) {
+    const int nt = k ? b->ntasks_r8 : b->ntasks;
+    if (nt == 0) continue;
+    const int sm = k ? b->smem_r8 : b->smem;
+    const void* kfn = b->arith == ARITH_F32 ? batch_kernel_f32(k == 1) : batch_kernel_f64(k == 1);
+    int per = 0;
+    if (cuda_check(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, sm), "batch attribute") ||
+        cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kfn, BATCH_THREADS, sm), "batch occupancy")) {
+      free_batch(b);
+      return nullptr;
+    }
+    (k ? b->grid_r8 : b->grid) = std::max(1, std::min(nt, std::max(1, per) * nsm));
+  }
+  if (b->ntasks > 0 && b->ntasks_r8 > 0 &&
+      (cuda_check(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking), "batch stream") ||
+       cuda_check(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming), "batch event") ||
+       cuda_check(cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming), "batch event"))) {
     free_batch(b);
     return nullptr;
   }
-  int dev = 0, nsm = 0, per = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kfn, BATCH_THREADS, b->smem);
-  b->grid = std::max(1, std::min(b->ntasks, std::max(1, per) * nsm));
+  tasks.insert(tasks.end(), tasks_r8.begin(), tasks_r8.end());
   if (cuda_check(cudaMalloc(&b->d_passes, sizeof(BatchPass) * hp.size()), "batch alloc") ||
-      cuda_check(cudaMalloc(&b->d_tasks, sizeof(BatchTask) * tasks.size()), "batch alloc") ||
-      cuda_check(cudaMalloc(&b->d_counters, sizeof(unsigned) * (b->ncounters + 1)), "batch alloc") ||
+      cuda_check(cudaMalloc(&b->d_tasks, sizeof(BatchTask) * std::max<size_t>(1, tasks.size())), "batch alloc") ||
+      cuda_check(cudaMalloc(&b->d_counters, sizeof(unsigned) * (b->ncounters + 2)), "batch alloc") ||
       cuda_check(cudaMalloc(&b->d_err, sizeof(int)), "batch alloc") ||
       cuda_check(cudaMallocHost(&b->h_err, sizeof(int)), "batch alloc")) {
     free_batch(b);
@@ -255,8 +321,8 @@ int pfft_gb300_batch_set_graph(pfft_gb300_batch batch, int on) {
 
 int pfft_gb300_batch_info(pfft_gb300_batch batch, int* ntasks, int* grid, int* threads, double* bytes) {
   if (!batch) return -1;
-  if (ntasks) *ntasks = batch->b->ntasks;
-  if (grid) *grid = batch->b->grid;
+  if (ntasks) *ntasks = batch->b->ntasks + batch->b->ntasks_r8;
+  if (grid) *grid = (batch->b->ntasks ? batch->b->grid : 0) + (batch->b->ntasks_r8 ? batch->b->grid_r8 : 0);
   if (threads) *threads = batch->b->threads;
   if (bytes) *bytes = batch->b->bytes;
   return 0;

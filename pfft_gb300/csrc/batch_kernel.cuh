@@ -181,9 +181,12 @@ __device__ __forceinline__ void batch_mixed(const BatchPass& bp, long long tile,
 
 // Float batches (DOUBLE = false) run FP32 tiles; in a double batch every
 // pass carries its own arithmetic (native FP64 for small plans, float-float
-// for large ones).
-template <bool DOUBLE>
-__global__ void __launch_bounds__(BATCH_THREADS, 3) k_batch(const BatchLaunch q) {
+// for large ones).  R8: the queue holds radix-8 tiles only (plans whose
+// passes all run on the radix-8 tile); that kernel carries no callee tiles
+// and fits four CTAs per SM (64 registers, the stand-alone kernel's budget)
+// instead of three.
+template <bool DOUBLE, bool R8>
+__global__ void __launch_bounds__(BATCH_THREADS, R8 ? 4 : 3) k_batch(const BatchLaunch q) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ int s_task;
   if (threadIdx.x == 0) s_task = (int)atomicAdd(q.next, 1u);
@@ -214,7 +217,9 @@ __global__ void __launch_bounds__(BATCH_THREADS, 3) k_batch(const BatchLaunch q)
     const long long tile = task.tile;
     unsigned char* sm = smraw;
     const bool neg = bp.p.sign < 0;
-    if (bp.fastN > 0 && bp.mixed) {
+    if constexpr (R8) {
+      batch_fast<DOUBLE>(bp, tile, sm);
+    } else if (bp.fastN > 0 && bp.mixed) {
       batch_mixed<DOUBLE>(bp, tile, sm);
     } else if (bp.fastN > 0) {
       batch_fast<DOUBLE>(bp, tile, sm);
@@ -248,10 +253,10 @@ __global__ void __launch_bounds__(BATCH_THREADS, 3) k_batch(const BatchLaunch q)
   }
 }
 
-// instantiation units batch_f32.cu / batch_f64.cu
-int batch_launch_f32(const BatchLaunch& q, int grid, int smem, cudaStream_t s);
-int batch_launch_f64(const BatchLaunch& q, int grid, int smem, cudaStream_t s);
-const void* batch_kernel_f32();
-const void* batch_kernel_f64();
+// instantiation units batch_f32.cu / batch_f64.cu (r8: the radix-8-only kernel)
+int batch_launch_f32(const BatchLaunch& q, int grid, int smem, cudaStream_t s, bool r8 = false);
+int batch_launch_f64(const BatchLaunch& q, int grid, int smem, cudaStream_t s, bool r8 = false);
+const void* batch_kernel_f32(bool r8 = false);
+const void* batch_kernel_f64(bool r8 = false);
 
 }  // namespace pg
