@@ -34,6 +34,7 @@ struct Batch {
   // its own persistent kernel at four CTAs per SM, tasks after the others in
   // d_tasks, ticket word after the general queue's
   int ntasks_r8 = 0, smem_r8 = 0, grid_r8 = 0;
+  int r8_kind = 1;  // k_batch's R8 for that queue: 1 any arithmetic, 2 TwoSum only, 3 block-quantised only
   cudaStream_t side = nullptr;  // the general queue's kernel runs here when both queues are used
   cudaEvent_t fork = nullptr, join = nullptr;
   int fast_passes = 0;
@@ -68,16 +69,16 @@ int launch_batch(Batch* b, cudaStream_t s) {
     q.ntasks = b->ntasks;
     q.next = b->d_counters + b->ncounters;
     cudaStream_t sg = both ? b->side : s;
-    rc = b->arith == ARITH_F32 ? batch_launch_f32(q, b->grid, b->smem, sg, false)
-                               : batch_launch_f64(q, b->grid, b->smem, sg, false);
+    rc = b->arith == ARITH_F32 ? batch_launch_f32(q, b->grid, b->smem, sg, 0)
+                               : batch_launch_f64(q, b->grid, b->smem, sg, 0);
     if (rc) return rc;
   }
   if (b->ntasks_r8 > 0) {
     q.tasks = b->d_tasks + b->ntasks;
     q.ntasks = b->ntasks_r8;
     q.next = b->d_counters + b->ncounters + 1;
-    rc = b->arith == ARITH_F32 ? batch_launch_f32(q, b->grid_r8, b->smem_r8, s, true)
-                               : batch_launch_f64(q, b->grid_r8, b->smem_r8, s, true);
+    rc = b->arith == ARITH_F32 ? batch_launch_f32(q, b->grid_r8, b->smem_r8, s, 1)
+                               : batch_launch_f64(q, b->grid_r8, b->smem_r8, s, b->r8_kind);
     if (rc) return rc;
   }
   if (both) {
@@ -201,6 +202,13 @@ Batch* make_batch(Plan* const* plans, int n) {
     }
   b->ntasks = (int)tasks.size();
   b->ntasks_r8 = (int)tasks_r8.size();
+  // double: the radix-8 queue's kernel carries only the arithmetic its plans use
+  if (b->arith != ARITH_F32) {
+    bool any_q = false, any_d = false;
+    for (int i = 0; i < n; i++)
+      if (r8[i]) (plans[i]->quant ? any_q : any_d) = true;
+    b->r8_kind = any_q && any_d ? 1 : (any_q ? 3 : 2);
+  }
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -208,7 +216,7 @@ Batch* make_batch(Plan* const* plans, int n) {
     const int nt = k ? b->ntasks_r8 : b->ntasks;
     if (nt == 0) continue;
     const int sm = k ? b->smem_r8 : b->smem;
-    const void* kfn = b->arith == ARITH_F32 ? batch_kernel_f32(k == 1) : batch_kernel_f64(k == 1);
+    const void* kfn = b->arith == ARITH_F32 ? batch_kernel_f32(k) : batch_kernel_f64(k ? b->r8_kind : 0);
     int per = 0;
     if (cuda_check(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, sm), "batch attribute") ||
         cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kfn, BATCH_THREADS, sm), "batch occupancy")) {

@@ -181,11 +181,13 @@ __device__ __forceinline__ void batch_mixed(const BatchPass& bp, long long tile,
 
 // Float batches (DOUBLE = false) run FP32 tiles; in a double batch every
 // pass carries its own arithmetic (native FP64 for small plans, float-float
-// for large ones).  R8: the queue holds radix-8 tiles only (plans whose
+// for large ones).  R8 > 0: the queue holds radix-8 tiles only (plans whose
 // passes all run on the radix-8 tile); that kernel carries no callee tiles
 // and fits four CTAs per SM (64 registers, the stand-alone kernel's budget)
-// instead of three.
-template <bool DOUBLE, bool R8>
+// instead of three.  R8 = 1 carries both double arithmetics, 2 only the
+// TwoSum tiles, 3 only the block-quantised ones (fewer code paths for the
+// register allocator).
+template <bool DOUBLE, int R8>
 __global__ void __launch_bounds__(BATCH_THREADS, R8 ? 4 : 3) k_batch(const BatchLaunch q) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ int s_task;
@@ -217,7 +219,11 @@ __global__ void __launch_bounds__(BATCH_THREADS, R8 ? 4 : 3) k_batch(const Batch
     const long long tile = task.tile;
     unsigned char* sm = smraw;
     const bool neg = bp.p.sign < 0;
-    if constexpr (R8) {
+    if constexpr (R8 == 3 && DOUBLE) {
+      batch_fast_p<fast::FQ>(bp, tile, sm);
+    } else if constexpr (R8 == 2 && DOUBLE) {
+      batch_fast_p<fast::FDD>(bp, tile, sm);
+    } else if constexpr (R8 > 0) {
       batch_fast<DOUBLE>(bp, tile, sm);
     } else if (bp.fastN > 0 && bp.mixed) {
       batch_mixed<DOUBLE>(bp, tile, sm);
@@ -253,10 +259,11 @@ __global__ void __launch_bounds__(BATCH_THREADS, R8 ? 4 : 3) k_batch(const Batch
   }
 }
 
-// instantiation units batch_f32.cu / batch_f64.cu (r8: the radix-8-only kernel)
-int batch_launch_f32(const BatchLaunch& q, int grid, int smem, cudaStream_t s, bool r8 = false);
-int batch_launch_f64(const BatchLaunch& q, int grid, int smem, cudaStream_t s, bool r8 = false);
-const void* batch_kernel_f32(bool r8 = false);
-const void* batch_kernel_f64(bool r8 = false);
+// instantiation units batch_f32.cu / batch_f64.cu (r8: the radix-8-only
+// kernel variant, k_batch's R8; float batches have variants 0 and 1)
+int batch_launch_f32(const BatchLaunch& q, int grid, int smem, cudaStream_t s, int r8 = 0);
+int batch_launch_f64(const BatchLaunch& q, int grid, int smem, cudaStream_t s, int r8 = 0);
+const void* batch_kernel_f32(int r8 = 0);
+const void* batch_kernel_f64(int r8 = 0);
 
 }  // namespace pg
