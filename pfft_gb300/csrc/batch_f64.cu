@@ -1,25 +1,34 @@
-// Kernel unit of the batched persistent launch (batch_kernel.cuh), double batches.
+// Double batches of the batched persistent launch: dispatch to the kernel
+// variant units batch_f64_r0.cu .. batch_f64_r3.cu (k_batch's R8).
 #include "batch_kernel.cuh"
 
 namespace pg {
 
+int batch_launch_f64_r0(const BatchLaunch& q, int grid, int smem, cudaStream_t s);
+int batch_launch_f64_r1(const BatchLaunch& q, int grid, int smem, cudaStream_t s);
+int batch_launch_f64_r2(const BatchLaunch& q, int grid, int smem, cudaStream_t s);
+int batch_launch_f64_r3(const BatchLaunch& q, int grid, int smem, cudaStream_t s);
+const void* batch_kernel_f64_r0();
+const void* batch_kernel_f64_r1();
+const void* batch_kernel_f64_r2();
+const void* batch_kernel_f64_r3();
+
 int batch_launch_f64(const BatchLaunch& q, int grid, int smem, cudaStream_t s, int r8) {
   switch (r8) {
-    case 1: k_batch<true, 1><<<grid, BATCH_THREADS, smem, s>>>(q); break;
-    case 2: k_batch<true, 2><<<grid, BATCH_THREADS, smem, s>>>(q); break;
-    case 3: k_batch<true, 3><<<grid, BATCH_THREADS, smem, s>>>(q); break;
-    default: k_batch<true, 0><<<grid, BATCH_THREADS, smem, s>>>(q); break;
+    case 1: return batch_launch_f64_r1(q, grid, smem, s);
+    case 2: return batch_launch_f64_r2(q, grid, smem, s);
+    case 3: return batch_launch_f64_r3(q, grid, smem, s);
   }
-  return (int)cudaGetLastError();
+  return batch_launch_f64_r0(q, grid, smem, s);
 }
 
 const void* batch_kernel_f64(int r8) {
   switch (r8) {
-    case 1: return (const void*)k_batch<true, 1>;
-    case 2: return (const void*)k_batch<true, 2>;
-    case 3: return (const void*)k_batch<true, 3>;
+    case 1: return batch_kernel_f64_r1();
+    case 2: return batch_kernel_f64_r2();
+    case 3: return batch_kernel_f64_r3();
   }
-  return (const void*)k_batch<true, 0>;
+  return batch_kernel_f64_r0();
 }
 
 }  // namespace pg
