@@ -17,14 +17,17 @@ needed between steps).
           of one launch over its CUDA-event duration, against the measured HBM
           copy bandwidth; traffic from the committed ncu summary
   cpu_baseline  the CPU oracle (a C FP64 port, not the reference, which cannot
-          be built: it needs FFTW-MPI and MPI) on the host cores, on a bounded
-          sample of the same workload
+          be built: it needs FFTW-MPI and MPI) on all host cores, one full
+          forward execute of the same 512^3 workload; scipy_baseline is
+          scipy.fft.fftn on the same input and cores (labelled: not the
+          reference)
   accuracy  round-trip relative L2 error (backward of the measured forward
           output, divided by N, against the input) and the Parseval defect of
           the measured transform; the double API's arithmetic is its default
           (float-float with block-quantised radix-8 stages at this size)
 
---impl reference times that CPU port instead (the reference arm).
+--impl reference times that CPU port instead (the reference arm): the full
+512^3 forward every step, with the real per-step wall time.
 With --gpus N > 1 (torchrun), every rank runs an independent replica (the path
 does not shard on one node without MPI); value sums the ranks' bytes over the
 slowest rank's time.
@@ -133,19 +136,48 @@ class Clocks:
                 "samples": len(sm), "power_w_median": statistics.median(pw) if pw else None}
 
 
-def cpu_baseline(sample_n0=128, threads=None):
-    """Time the CPU oracle on a bounded sample (n0 x 512 x 512) of the workload."""
+def _oracle_forward(n, x, threads):
     import oracle
+    cnt = 2 * int(np.prod(n))
+    return oracle.execute("c2c", n, n, n, 1, -1, 0, 2, x, cnt, nthreads=threads)
+
+
+def cpu_input(n, seed=1):
+    return np.random.default_rng(seed).uniform(-1.0, 1.0, 2 * int(np.prod(n)))
+
+
+def cpu_baseline(n=N3, threads=None, x=None):
+    """Time the CPU oracle on one full forward execute of the workload (the
+    whole 512^3 complex128 transform, about 3 s on 16 cores)."""
     threads = threads or (os.cpu_count() or 1)
-    n = (sample_n0, N3[1], N3[2])
-    rng = np.random.default_rng(1)
-    x = rng.uniform(-1.0, 1.0, 2 * int(np.prod(n)))
+    x = cpu_input(n) if x is None else x
     t0 = time.perf_counter()
-    oracle.execute("c2c", n, n, n, 1, -1, 0, 2, x, 2 * int(np.prod(n)), nthreads=threads)
+    _oracle_forward(n, x, threads)
     dt = time.perf_counter() - t0
     return {"value": algo_bytes(n) / dt / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
-            "sample": "%dx512x512 c2c complex128 forward (1/%d of the workload), one run, %.2f s" %
-                      (sample_n0, N3[0] // sample_n0, dt)}
+            "sample": "the full workload: one %s c2c complex128 forward, %.2f s" % ("x".join(map(str, n)), dt),
+            "seconds": dt}
+
+
+def scipy_baseline(n=N3, threads=None, x=None, reps=1):
+    """scipy.fft.fftn (pocketfft, not the reference and not FFTW) on the same
+    input with all host threads: a second, independent CPU number."""
+    try:
+        import scipy.fft as sf
+    except Exception as e:  # pragma: no cover - scipy is on both machines
+        return {"unavailable": "scipy.fft not importable: %s" % e}
+    threads = threads or (os.cpu_count() or 1)
+    x = cpu_input(n) if x is None else x
+    z = x.view(np.complex128).reshape(n)
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        sf.fftn(z, workers=threads)
+        ts.append(time.perf_counter() - t0)
+    dt = statistics.median(ts)
+    return {"value": algo_bytes(n) / dt / 1e9, "unit": "GB/s", "cores": threads, "kind": "scipy",
+            "sample": "scipy.fft.fftn(workers=%d) of the full %s complex128 input, median of %d, %.2f s; "
+                      "not the reference" % (threads, "x".join(map(str, n)), reps, dt)}
 
 
 BATCH_SIZES = [(32, 32, 32), (48, 64, 40), (96, 96, 96), (128, 128, 64), (128, 128, 128)]
@@ -298,28 +330,43 @@ def barrier(world):
 
 
 def run_reference(args, world, rank):
+    """The reference arm: the reference (PFFT + FFTW-MPI + MPI) cannot be
+    built here, so this times its CPU restatement (the oracle, FP64) on the
+    same workload as the GPU arm - one full 512^3 complex128 forward execute
+    per step, all host threads - with the real per-step wall time."""
     if rank != 0:
         return
-    steps = []
     threads = os.cpu_count() or 1
+    n = (args.ref_n,) * 3
+    x = cpu_input(n)
+    per = []
+    t_all = time.perf_counter()
     for i in range(args.warmup + args.steps):
-        r = cpu_baseline(sample_n0=args.ref_sample_n0, threads=threads)
+        t0 = time.perf_counter()
+        _oracle_forward(n, x, threads)
+        dt = time.perf_counter() - t0
         if i >= args.warmup:
-            steps.append(r)
-    v = statistics.median([s["value"] for s in steps])
-    ms = algo_bytes() / (v * 1e9) * 1e3
+            per.append(dt)
+    wall = time.perf_counter() - t_all
+    ms = 1e3 * sum(per) / len(per)
+    v = algo_bytes(n) / (ms * 1e-3) / 1e9
     line = {"metric": "3D FFT HBM GB/s & %roofline, 5N*log2N GFLOP/s; batched vs loop; adjoint cost",
             "value": v, "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic uniform[-1,1) seed 1",
-            "config": {"workload": "pfft_execute c2c 512^3 complex128 forward, 1x1 procmesh, out-of-place "
-                                   "(CPU port timed on a %dx512x512 sample per step)" % args.ref_sample_n0},
+            "config": {"workload": "pfft_execute c2c %d^3 complex128 forward, 1x1 procmesh, out-of-place, "
+                                   "TRANSPOSED_NONE" % args.ref_n,
+                       "bytes_per_step": algo_bytes(n), "p_min": P_MIN, "parallelism": "host cores"},
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "GB/s", "cores": threads, "kind": "port",
-                             "sample": steps[0]["sample"]},
+                             "sample": "the full workload every step: %d timed + %d warm-up forward executes "
+                                       "of %d^3 complex128, mean %.2f s per step, %.1f s in all" %
+                                       (args.steps, args.warmup, args.ref_n, ms / 1e3, wall)},
             "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "the reference (PFFT + FFTW-MPI + MPI) cannot be built here; this arm times the CPU "
                     "oracle, a C FP64 restatement of its transform path"}
+    if not args.no_scipy:
+        line["scipy_baseline"] = scipy_baseline(n, threads, x)
     print(json.dumps(line), flush=True)
 
 
@@ -331,7 +378,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the batched-vs-loop and adjoint-cost parts")
-    ap.add_argument("--ref-sample-n0", type=int, default=128)
+    ap.add_argument("--no-scipy", action="store_true", help="skip the scipy.fft.fftn CPU number")
+    ap.add_argument("--ref-n", type=int, default=512,
+                    help="cube edge of the reference arm's workload (512, the benchmark's; smaller only in tests)")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--n", type=int, default=512, help="cube edge (profiling runs use a smaller case)")
     ap.add_argument("--shape", default=None, help="n0xn1xn2 instead of a cube (profiling runs)")
@@ -513,7 +562,10 @@ def main():
     }
     line.update(extra)
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(sample_n0=args.ref_sample_n0)
+        xb = cpu_input(N3)
+        line["cpu_baseline"] = cpu_baseline(N3, x=xb)
+        if not args.no_scipy:
+            line["scipy_baseline"] = scipy_baseline(N3, x=xb)
     print(json.dumps(line), flush=True)
 
 

@@ -169,13 +169,17 @@ int pfft_gb300_staged_status(void);
  * 3-D block of n[0] x n[1] x n[2] cells with `tuple` reals per cell (1 for
  * real data, 2 for complex, times howmany) stored at the start of `data`,
  * expanded in place into the (gc_below + n + gc_above) box.  precision: 1 =
- * double, 0 = float.  `data` must be device or managed memory; `stream` is a
- * cudaStream_t (NULL: the legacy default stream); the call only queues work.
+ * double, 0 = float.  `data` must be managed memory or device memory of the
+ * current device (another GPU's pointer: cudaErrorInvalidDevice, host
+ * memory: cudaErrorInvalidValue); `stream` is a cudaStream_t (NULL: the
+ * legacy default stream); the call only queues work.
  * Scratch: a fixed 32 MiB array in the library's device image (every GPU that
  * loads this code holds it until exit); blocks larger than 32 MiB are refused
- * (cudaErrorMemoryAllocation returned, nothing queued).  The first call on a
- * device looks up the array's device address; make that first call before
- * any stream capture.  All calls share the array: calls whose GPU work
+ * (cudaErrorMemoryAllocation returned, nothing queued), and so are sizes
+ * whose products overflow.  The first call on a device looks up the array's
+ * device address and the SM count; make that first call before any stream
+ * capture.  After cudaDeviceReset, call pfft_cleanup() so that the next call
+ * looks them up again.  All calls share the array: calls whose GPU work
  * overlaps (different streams, no ordering) race.  Returns 0 or a
  * cudaError_t value. */
 int pfft_gb300_exchange_noalloc(int precision, const ptrdiff_t *n, const ptrdiff_t *gc_below,

@@ -34,7 +34,8 @@ struct Batch {
   // its own persistent kernel at four CTAs per SM, tasks after the others in
   // d_tasks, ticket word after the general queue's
   int ntasks_r8 = 0, smem_r8 = 0, grid_r8 = 0;
-  int r8_kind = 1;  // k_batch's R8 for that queue: 1 any arithmetic, 2 TwoSum only, 3 block-quantised only
+  int r8_kind = 1;  // k_batch's R8 for that queue: 1 any arithmetic, 2 TwoSum only, 3 block-quantised only,
+                    // 4 64-bit fixed point only
   cudaStream_t side = nullptr;  // the general queue's kernel runs here when both queues are used
   cudaEvent_t fork = nullptr, join = nullptr;
   int fast_passes = 0;
@@ -204,10 +205,11 @@ Batch* make_batch(Plan* const* plans, int n) {
   b->ntasks_r8 = (int)tasks_r8.size();
   // double: the radix-8 queue's kernel carries only the arithmetic its plans use
   if (b->arith != ARITH_F32) {
-    bool any_q = false, any_d = false;
+    bool any_q = false, any_d = false, any_x = false;
     for (int i = 0; i < n; i++)
-      if (r8[i]) (plans[i]->quant ? any_q : any_d) = true;
-    b->r8_kind = any_q && any_d ? 1 : (any_q ? 3 : 2);
+      if (r8[i]) (plans[i]->quant == 2 ? any_x : plans[i]->quant ? any_q : any_d) = true;
+    const int kinds = (int)any_q + (int)any_d + (int)any_x;
+    b->r8_kind = kinds > 1 ? 1 : (any_x ? 4 : (any_q ? 3 : 2));
   }
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);

@@ -107,12 +107,15 @@ __device__ __forceinline__ void batch_fast_p(const BatchPass& bp, long long tile
   }
 }
 
-// double batches: the arithmetic of the pass's plan (TwoSum or
-// block-quantised float-float radix-8 stages, PassParams::quant)
+// double batches: the arithmetic of the pass's plan (PassParams::quant: 64-bit
+// fixed point for double plans, TwoSum or block-quantised float-float
+// radix-8 stages for float-float plans)
 template <bool DOUBLE>
 __device__ __forceinline__ void batch_fast(const BatchPass& bp, long long tile, unsigned char* sm) {
   if constexpr (DOUBLE) {
-    if (bp.p.quant)
+    if (bp.p.quant == 2)
+      batch_fast_p<fast::FX>(bp, tile, sm);
+    else if (bp.p.quant)
       batch_fast_p<fast::FQ>(bp, tile, sm);
     else
       batch_fast_p<fast::FDD>(bp, tile, sm);
@@ -184,9 +187,9 @@ __device__ __forceinline__ void batch_mixed(const BatchPass& bp, long long tile,
 // for large ones).  R8 > 0: the queue holds radix-8 tiles only (plans whose
 // passes all run on the radix-8 tile); that kernel carries no callee tiles
 // and fits four CTAs per SM (64 registers, the stand-alone kernel's budget)
-// instead of three.  R8 = 1 carries both double arithmetics, 2 only the
-// TwoSum tiles, 3 only the block-quantised ones (fewer code paths for the
-// register allocator).
+// instead of three.  R8 = 1 carries every double arithmetic, 2 only the
+// TwoSum tiles, 3 only the block-quantised ones, 4 only the 64-bit
+// fixed-point ones (fewer code paths for the register allocator).
 template <bool DOUBLE, int R8>
 __global__ void __launch_bounds__(BATCH_THREADS, R8 ? 4 : 3) k_batch(const BatchLaunch q) {
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -219,7 +222,9 @@ __global__ void __launch_bounds__(BATCH_THREADS, R8 ? 4 : 3) k_batch(const Batch
     const long long tile = task.tile;
     unsigned char* sm = smraw;
     const bool neg = bp.p.sign < 0;
-    if constexpr (R8 == 3 && DOUBLE) {
+    if constexpr (R8 == 4 && DOUBLE) {
+      batch_fast_p<fast::FX>(bp, tile, sm);
+    } else if constexpr (R8 == 3 && DOUBLE) {
       batch_fast_p<fast::FQ>(bp, tile, sm);
     } else if constexpr (R8 == 2 && DOUBLE) {
       batch_fast_p<fast::FDD>(bp, tile, sm);

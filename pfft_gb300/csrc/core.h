@@ -81,6 +81,8 @@ int effective_mesh_rank(int rnk_n, int cart_dims);
 // ---- twiddle tables (twiddle.cpp) ----------------------------------------
 const void* twiddle_table(int M, int arith, cudaError_t* err);
 void twiddle_release_all();
+// forget the allocation-free exchange's per-device set-up (gcell_noalloc.cu)
+void noalloc_forget();
 
 // ---- array layouts ------------------------------------------------------------
 #define PG_MAX_DIMS 7
@@ -146,6 +148,10 @@ struct Plan {
   void* in = nullptr;   // planned arrays
   void* out = nullptr;
   bool inplace = false;
+  // PFFT_BUFFERED_INPLACE on an out-of-place plan: the transform runs as an
+  // in-place program on the input array (results end up in it); the output
+  // array is never written (plan.cpp, make_plan)
+  bool buffered = false;
   PassProgram fwd;      // the transform
   PassProgram adj;      // its adjoint (built on demand)
   bool adj_built = false;
@@ -196,9 +202,10 @@ Plan* make_plan(const PlanDesc& base, void* in, void* out);
 void execute_plan(Plan* pl, void* in, void* out, bool adjoint);
 void destroy_plan(Plan* pl);
 
-// arithmetic policy of the double API: float-float, native FP64, or by size
+// arithmetic policy of the double API (plan.cpp, plan_double_arith): the
+// default keeps FFTW-class answers (64-bit fixed point on the radix-8 passes,
+// FP64 elsewhere); native FP64 everywhere; or the opt-in float-float forms
 enum { DARITH_DF = 0, DARITH_NATIVE = 1, DARITH_AUTO = 2, DARITH_DFQ = 3 };
-constexpr long long DARITH_AUTO_POINTS = 1LL << 18;
 int double_arith();
 void set_double_arith(int a);
 int plan_double_arith(const PlanDesc& d);

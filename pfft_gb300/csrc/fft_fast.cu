@@ -138,7 +138,9 @@ static bool fast_tables(const PassParams& p, int arith, bool pow2, const void** 
   cudaError_t e;
   const bool dct = p.mode == MODE_RE10 || p.mode == MODE_RE01;
   const int fsign = p.mode == MODE_RE10 ? -1 : (p.mode == MODE_RE01 ? 1 : p.sign);
-  if (arith == ARITH_DF) {
+  if (arith == ARITH_F64) {  // 64-bit fixed point (FX), plain power-of-two c2c only
+    *tw = twiddle_table(p.N, fsign < 0 ? TW_FX_FWD_STG : TW_FX_BWD_STG, &e);
+  } else if (arith == ARITH_DF) {
     *tw = twiddle_table(p.N, pow2 ? (fsign < 0 ? TW_DFP_FWD_STG : TW_DFP_BWD_STG) : (fsign < 0 ? TW_DFP_FWD : TW_DFP_BWD),
                         &e);
     if (dct) *tw2 = twiddle_table(p.M, fsign < 0 ? TW_DFP_FWD : TW_DFP_BWD, &e);
@@ -160,7 +162,12 @@ bool fast_args(const PassParams& p, int arith, FastArgs* a, bool* row_in, bool* 
   // the mixed-radix kernel reads and writes plain c2c lines only
   if (!pow2 && (!mixed_supported(N) || !plain)) return false;
   if ((p.mode == MODE_RE10 || p.mode == MODE_RE01) && N > 512) return false;
-  if (arith != ARITH_F32 && arith != ARITH_DF) return false;
+  // double plans (native FP64 storage and arithmetic class): the radix-8
+  // kernel's 64-bit fixed-point arithmetic on plain power-of-two c2c lines
+  // (PassParams::quant == 2); every other pass of such a plan runs the
+  // general kernel in FP64
+  if (arith == ARITH_F64 && !(p.quant == 2 && pow2 && plain)) return false;
+  if (arith != ARITH_F32 && arith != ARITH_DF && arith != ARITH_F64) return false;
   if (p.ashI.en || p.ashO.en) return false;
   if (p.nb > PG_MAX_BATCH) return false;
   for (int b = 0; b < p.nb; b++)
@@ -262,6 +269,11 @@ int launch_fast_pass(const PassParams& p, int arith, cudaStream_t stream) {
     if (sign < 0)
       return big ? launch_large<F32, -1>(N, a, row_in, row_out, stream) : launch_small<F32, -1>(N, a, row_in, row_out, stream);
     return big ? launch_large<F32, 1>(N, a, row_in, row_out, stream) : launch_small<F32, 1>(N, a, row_in, row_out, stream);
+  }
+  if (arith == ARITH_F64) {  // 64-bit fixed-point radix-8 stages (fast_args admitted plain c2c only)
+    if (sign < 0)
+      return big ? launch_large<FX, -1>(N, a, row_in, row_out, stream) : launch_small<FX, -1>(N, a, row_in, row_out, stream);
+    return big ? launch_large<FX, 1>(N, a, row_in, row_out, stream) : launch_small<FX, 1>(N, a, row_in, row_out, stream);
   }
   if (p.quant) {  // block-quantised float-float radix-8 stages
     if (sign < 0)

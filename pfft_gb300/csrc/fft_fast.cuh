@@ -20,6 +20,7 @@
 //     renormalised only when written to global memory.
 // A length N = 8^a * q (q = 1, 2, 4) runs a radix-8 stages and one radix-q stage.
 #pragma once
+#include <limits.h>
 #include <algorithm>
 #include <type_traits>
 #include "arith.cuh"
@@ -45,6 +46,7 @@ struct F32 {
   static __device__ __forceinline__ C swap_neg_re(C a) { return make_float2(-a.y, a.x); }  // *i
   static __device__ __forceinline__ C swap_neg_im(C a) { return make_float2(a.y, -a.x); }  // *(-i)
   static __device__ __forceinline__ C renorm(C a) { return a; }
+  static __device__ __forceinline__ C tw0(C a) { return a; }
   static __device__ __forceinline__ C ld(const G* p) { return *p; }
   static __device__ __forceinline__ void st(G* p, C v) { *p = v; }
   static __device__ __forceinline__ C lds(const S& s) { return s; }
@@ -180,6 +182,7 @@ struct FDD {
     const float2 s = add2(a.h, a.l);
     return {s, sub2(a.l, sub2(s, a.h))};
   }
+  static __device__ __forceinline__ C tw0(C a) { return a; }
   static __device__ __forceinline__ C from_df(df re, df im) {
     return {make_float2(re.hi, im.hi), make_float2(re.lo, im.lo)};
   }
@@ -350,6 +353,146 @@ __device__ __forceinline__ void bf8x(typename P::C* v) {
     bf8<P, SIGN>(v);
 }
 
+// ---- 64-bit block-fixed-point arithmetic (double API) -------------------------
+// FX: the double API's arithmetic of the radix-8 kernel.  A tile's values
+// are converted, after loading, to 64-bit integers on one grid common to the
+// tile: with E the largest biased exponent of the tile's doubles, a double
+// m * 2^(e - 1075) (53-bit mantissa m) becomes X = (m << 5) >> (E - e), so
+// x = X * 2^(E - 1080) and |X| < 2^58: 58 significant bits against the
+// tile's largest component (a double holds 53 against its own magnitude).
+// Additions and subtractions are exact 64-bit integer operations.  Every
+// stage but the first multiplies by twiddles scaled by 1/8 (element 0 of a
+// butterfly, whose twiddle is 1, is shifted right by 3), which cancels the
+// radix-8 stage's growth: a butterfly's inputs have modulus below 2^58.5,
+// its partial sums and outputs below 2^61.5, the twiddle product's sum
+// a.re + a.im below 2^62.5 < 2^63, so nothing overflows.  Products are
+// 64 x 64 -> high 64 bits from 32-bit pieces (fx_mh: the low-by-low part and
+// the carries of the cross terms are dropped, error within 2 units of the
+// result), complex products in Gauss's three-multiplication form, the
+// sqrt(1/2) products of the butterflies as a - a (1 - sqrt(1/2)).  Every
+// rounding is a few units at 2^-58 of the tile's magnitude, below the
+// 2^-53 relative rounding of FP64 arithmetic.  Results are rounded to
+// nearest double when stored (x = Y * 2^(E - 1080 + 3 * twiddled stages)).
+// A tile holding an infinity or NaN stores NaN everywhere; results below
+// 2^-1022 are stored as zero.
+struct FX {
+  typedef longlong2 S;  // shared memory: (re, im)
+  typedef double2 G;
+  struct C {
+    long long x, y;
+  };
+  // twiddle w / 8 (stored as (hi, lo) with lo in [-2^31, 2^31), value hi * 2^32
+  // + lo, scaled by 2^64): r = Re w, d = Im w - Re w, s = Re w + Im w
+  struct W {
+    int2 r, d, s;
+  };
+  struct K8 {};  // tag of the sqrt(1/2) constant
+  static __device__ __forceinline__ C add(C a, C b) { return {a.x + b.x, a.y + b.y}; }
+  static __device__ __forceinline__ C sub(C a, C b) { return {a.x - b.x, a.y - b.y}; }
+  static __device__ __forceinline__ C neg(C a) { return {-a.x, -a.y}; }
+  static __device__ __forceinline__ C swap_neg_re(C a) { return {-a.y, a.x}; }  // * i
+  static __device__ __forceinline__ C swap_neg_im(C a) { return {a.y, -a.x}; }  // * (-i)
+  static __device__ __forceinline__ C renorm(C a) { return a; }
+  static __device__ __forceinline__ C conj(C a) { return {a.x, -a.y}; }
+  static __device__ __forceinline__ C lds(const S& s) { return {s.x, s.y}; }
+  static __device__ __forceinline__ S sts(C v) { return make_longlong2(v.x, v.y); }
+  // floor(x * w / 2^64) up to a few units: x = xh 2^32 + xl, w = wh 2^32 + wl
+  // with signed low halves; the cross terms' high words and xh * wh
+  static __device__ __forceinline__ long long mh(long long x, int2 w) {
+    const unsigned xu = (unsigned)x;
+    const int xl = (int)xu;
+    const int xh = (int)(x >> 32) + (int)(xu >> 31);
+    const long long c = (long long)__mulhi(xh, w.y) + (long long)__mulhi(xl, w.x) + 1;
+    return (long long)xh * w.x + c;
+  }
+  static __device__ __forceinline__ C mul(C a, const W& w) {
+    const long long k1 = mh(a.x + a.y, w.r);
+    const long long k2 = mh(a.x, w.d);
+    const long long k3 = mh(a.y, w.s);
+    return {k1 - k3, k1 + k2};
+  }
+  static __device__ __forceinline__ K8 c8() { return {}; }
+  static __device__ __forceinline__ C scal(C a, K8) {
+    const int2 k = make_int2(1257966796, 102865788);  // (1 - sqrt(1/2)) 2^64
+    return {a.x - mh(a.x, k), a.y - mh(a.y, k)};
+  }
+  // element 0 of a twiddled stage (twiddle 1, scaled by 1/8)
+  static __device__ __forceinline__ C tw0(C a) { return {a.x >> 3, a.y >> 3}; }
+  static __device__ __forceinline__ W ldw(const void* base, int idx, int cnt) {
+    const int2* t = (const int2*)base;
+    return {__ldg(t + idx), __ldg(t + cnt + idx), __ldg(t + 2 * cnt + idx)};
+  }
+  template <int SIGN>
+  static __device__ __forceinline__ W twd(const W& w) {
+    return w;  // direction-specific tables
+  }
+};
+template <class P>
+__host__ __device__ constexpr bool is_fx() {
+  return std::is_same<P, FX>::value;
+}
+
+// double bits -> X on the tile grid of largest biased exponent E (E >= 1)
+__device__ __forceinline__ long long fx_from_bits(long long b, int E) {
+  const unsigned long long u = (unsigned long long)b;
+  const int e = (int)(u >> 52) & 0x7FF;
+  const unsigned long long m = (u & 0xFFFFFFFFFFFFFull) | (e ? (1ull << 52) : 0ull);
+  const int d = min(E - max(e, 1), 63);
+  const long long X = (long long)((m << 5) >> d);
+  return b < 0 ? -X : X;
+}
+// Y * 2^eo rounded to the nearest double, as bits; eo == INT_MIN: NaN
+__device__ __forceinline__ double fx_to_double(long long Y, int eo) {
+  if (eo == INT_MIN) return __longlong_as_double(0x7FF8000000000000ll);
+  const unsigned long long sgn = (unsigned long long)Y & 0x8000000000000000ull;
+  const unsigned long long a = Y < 0 ? (unsigned long long)(-Y) : (unsigned long long)Y;
+  if (a == 0) return 0.0;
+  const int lz = __clzll((long long)a);
+  const unsigned long long n = a << lz;  // bit 63 set
+  unsigned long long mant = n >> 11;
+  const unsigned rem = (unsigned)n & 0x7FFu;
+  mant += (rem > 0x400u || (rem == 0x400u && (mant & 1ull))) ? 1ull : 0ull;
+  int eb = eo + 1086 - lz;
+  if (mant >> 53) {
+    mant >>= 1;
+    eb++;
+  }
+  if (eb <= 0) return __longlong_as_double((long long)sgn);  // below 2^-1022: zero
+  if (eb >= 2047) return __longlong_as_double((long long)(sgn | 0x7FF0000000000000ull));
+  return __longlong_as_double((long long)(sgn | ((unsigned long long)eb << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+}
+// The tile's entry into FX: v holds the thread's eight values as double bits
+// (gload<FX>); every thread of the block takes part (one barrier).  Returns
+// the exponent of the stored results (fx_to_double) for a length-N line.
+template <int N>
+__device__ __forceinline__ int fx_enter(FX::C (&v)[8], int conj_in) {
+  __shared__ unsigned red[32];
+  unsigned em = 0;
+#pragma unroll
+  for (int r = 0; r < 8; r++) {
+    em = max(em, (unsigned)(v[r].x >> 32) & 0x7FF00000u);
+    em = max(em, (unsigned)(v[r].y >> 32) & 0x7FF00000u);
+  }
+  em = __reduce_max_sync(0xffffffffu, em);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) red[warp] = em;
+  __syncthreads();
+  em = lane < (int)(blockDim.x >> 5) ? red[lane] : 0u;
+  em = __reduce_max_sync(0xffffffffu, em);
+  const int Eraw = (int)(em >> 20);
+  const int E = max(Eraw, 1);
+#pragma unroll
+  for (int r = 0; r < 8; r++) {
+    v[r].x = fx_from_bits(v[r].x, E);
+    v[r].y = fx_from_bits(v[r].y, E);
+    if (conj_in) v[r].y = -v[r].y;
+  }
+  constexpr int NS8 = N >= 4096 ? 4 : (N >= 512 ? 3 : (N >= 64 ? 2 : 1));
+  constexpr int P8 = NS8 == 4 ? 4096 : (NS8 == 3 ? 512 : (NS8 == 2 ? 64 : 8));
+  constexpr int TWST = NS8 - 1 + (N / P8 > 1 ? 1 : 0);  // stages with (scaled) twiddles
+  return Eraw == 0x7FF ? INT_MIN : E - 1080 + 3 * TWST;
+}
+
 // Shared-memory layout of a tile: L lines at stride lsp_of, element p of a
 // line at index pad(p).  The layouts below make every stage exchange of the
 // kernel free of bank conflicts; they were chosen by simulating the
@@ -447,6 +590,17 @@ template <>
 __device__ __forceinline__ FDD::C gload<FQ, false>(const FDD::G* p, int df) { return gload_fdd<false>(p, df); }
 template <>
 __device__ __forceinline__ FDD::C gload<FQ, true>(const FDD::G* p, int df) { return gload_fdd<true>(p, df); }
+// FX: the raw bits of the doubles (converted by fx_enter)
+template <>
+__device__ __forceinline__ FX::C gload<FX, false>(const FX::G* p, int) {
+  const double2 v = *p;
+  return {__double_as_longlong(v.x), __double_as_longlong(v.y)};
+}
+template <>
+__device__ __forceinline__ FX::C gload<FX, true>(const FX::G* p, int) {
+  const double2 v = __ldcg(p);
+  return {__double_as_longlong(v.x), __double_as_longlong(v.y)};
+}
 template <class P>
 __device__ __forceinline__ void gstore(typename P::G* p, typename P::C v, int df);
 template <>
@@ -463,6 +617,11 @@ __device__ __forceinline__ void gstore<FDD>(FDD::G* p, FDD::C v, int df) {
 template <>
 __device__ __forceinline__ void gstore<FQ>(FDD::G* p, FDD::C v, int df) {
   gstore<FDD>(p, v, df);
+}
+// FX: `df` carries the exponent of the results (fx_enter)
+template <>
+__device__ __forceinline__ void gstore<FX>(FX::G* p, FX::C v, int eo) {
+  *p = make_double2(fx_to_double(v.x, eo), fx_to_double(v.y, eo));
 }
 
 // real-array element access (r2c input, c2r output)
@@ -610,7 +769,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsi
 #pragma unroll
     for (int r = 0; r < 8; r++) {
       v[r] = gload<P, CG>(src + r * st, a.in_df);
-      if (a.conj_in) v[r] = P::conj(v[r]);
+      if (!is_fx<P>() && a.conj_in) v[r] = P::conj(v[r]);  // FX: in fx_enter
     }
   } else {
 #pragma unroll
@@ -639,6 +798,8 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
   const void* tw = a.tw;  // stage-major table (TW_F32_STG, TW_DFP_*_STG)
   constexpr int TWN = fast_tw_n(N);
   S* line = buf + l * LSP;
+  int sdf = a.out_df;  // FX: the results' exponent instead
+  if constexpr (is_fx<P>()) sdf = fx_enter<N>(v, a.conj_in);
   bf8x<P, SIGN>(v);  // stage 0 (Ns = 1, no twiddles)
   int Ns = 1;
   // radix-8 stages 1 .. NS8-1 through shared memory
@@ -656,6 +817,7 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
 #pragma unroll
     for (int r = 0; r < 8; r++) v[r] = P::lds(line[pad<P>(t + r * TPL)]);
     const int k = t % Ns;
+    v[0] = P::tw0(v[0]);
 #pragma unroll
     for (int r = 1; r < 8; r++) v[r] = P::mul(v[r], P::template twd<SIGN>(P::ldw(tw, Ns - 8 + (r - 1) * Ns + k, TWN)));
     bf8x<P, SIGN>(v);
@@ -668,7 +830,7 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
           G* dst = (G*)a.dst + offO[l] + (long long)t * a.sOa;
           const long long st = (long long)TPL * a.sOa;
 #pragma unroll
-          for (int r = 0; r < 8; r++) gstore<P>(dst + r * st, a.conj_out ? P::conj(v[r]) : v[r], a.out_df);
+          for (int r = 0; r < 8; r++) gstore<P>(dst + r * st, a.conj_out ? P::conj(v[r]) : v[r], sdf);
         } else {
 #pragma unroll
           for (int r = 0; r < 8; r++) store_elem<P, IO == 2>(a, offO[l], t + r * TPL, v[r], N);
@@ -698,7 +860,7 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
 #pragma unroll
       for (int r = 0; r < Q; r++) {
         C x = P::lds(line[pad<P>(j + r * NQ)]);
-        if (r > 0) x = P::mul(x, P::template twd<SIGN>(P::ldw(tw, NQ - 8 + (r - 1) * NQ + j, TWN)));
+        x = r > 0 ? P::mul(x, P::template twd<SIGN>(P::ldw(tw, NQ - 8 + (r - 1) * NQ + j, TWN))) : P::tw0(x);
         w[b * Q + r] = x;
       }
       if (Q == 2) {
@@ -718,7 +880,7 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
 #pragma unroll
             for (int r = 0; r < Q; r++) {
               C o = a.conj_out ? P::conj(w[b * Q + r]) : w[b * Q + r];
-              gstore<P>(dst + (long long)(t + b * TPL + r * NQ) * a.sOa, o, a.out_df);
+              gstore<P>(dst + (long long)(t + b * TPL + r * NQ) * a.sOa, o, sdf);
             }
         } else {
 #pragma unroll
@@ -749,7 +911,7 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
         C o = P::lds(line2[pad<P>(k)]);
         if constexpr (IO == 0) {
           if (a.conj_out) o = P::conj(o);
-          gstore<P>(d2 + (long long)k * a.sOa, o, a.out_df);
+          gstore<P>(d2 + (long long)k * a.sOa, o, sdf);
         } else {
           store_elem<P, IO == 2>(a, offO[l2], k, o, N);
         }
@@ -932,7 +1094,7 @@ template <class P, int SIGN, int N, int L, int IO = 0>
 int launch4(const FastArgs& a, bool row_in, bool row_out, cudaStream_t s) {
   constexpr int T = L * (N / 8);
   const size_t smem = fast_smem_bytes<P, N, L>();
-  if constexpr (IO == 0 && staged_smem_bytes<P, N, L>() <= 227 * 1024) {
+  if constexpr (IO == 0 && !is_fx<P>() && staged_smem_bytes<P, N, L>() <= 227 * 1024) {
     CUtensorMap tm;
     if (staged_setup(a, N, L, (int)sizeof(typename P::G), row_in, &tm)) {
       if (row_in && row_out) return launch_staged<P, SIGN, N, L, true, true>(a, tm, s);

@@ -290,7 +290,10 @@ void write_info(FILE* f, const Plan* p) {
 #define PG_HELPERS(PX, R, C)                                                                              \
   extern "C" {                                                                                            \
   void PX##init(void) { cudaFree(0); }                                                                    \
-  void PX##cleanup(void) { twiddle_release_all(); }                                                       \
+  void PX##cleanup(void) {                                                                              \
+    twiddle_release_all();                                                                                \
+    noalloc_forget();                                                                                     \
+  }                                                                                                       \
   void PX##plan_with_nthreads(int n) { g_nthreads = n > 0 ? n : 1; }                                      \
   int PX##get_nthreads(void) { return g_nthreads; }                                                       \
   void* PX##malloc(size_t n) {                                                                            \

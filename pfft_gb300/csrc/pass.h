@@ -23,7 +23,19 @@ enum ArithId { ARITH_F32 = 0, ARITH_F64 = 1, ARITH_DF = 2 };
 //     threads (consecutive k or j) read consecutive entries.
 // Packed tables are stored as two arrays of float4: all high parts, then all
 // low parts (FDD::W).
-enum TwiddleKind { TW_DFP_FWD = 16, TW_DFP_BWD = 17, TW_F32_STG = 18, TW_DFP_FWD_STG = 19, TW_DFP_BWD_STG = 20 };
+//   TW_FX_FWD_STG / _BWD_STG: the radix-8 kernel's stage-major tables for the
+//     64-bit fixed-point arithmetic (FX::W): three arrays of int2, Re w,
+//     Im w - Re w and Re w + Im w, each scaled by 2^61 (w / 8 in units of
+//     2^-64) and split as hi * 2^32 + lo with lo in [-2^31, 2^31).
+enum TwiddleKind {
+  TW_DFP_FWD = 16,
+  TW_DFP_BWD = 17,
+  TW_F32_STG = 18,
+  TW_DFP_FWD_STG = 19,
+  TW_DFP_BWD_STG = 20,
+  TW_FX_FWD_STG = 21,
+  TW_FX_BWD_STG = 22
+};
 // entries of a stage-major table for a power-of-two N >= 16
 inline int fast_tw_count(int N) {
   int p8 = 8;
@@ -100,8 +112,10 @@ struct PassParams {
   int staged;   // staged variant of the radix-8 kernel (plain c2c passes): 0 default
                 // (float column passes), 1 on where the layout allows, 2 off
   int quant;    // double API, plain c2c passes of the radix-8 and mixed-radix
-                // kernels: float-float with block-quantised high words (1) instead
-                // of TwoSum additions (0)
+                // kernels: float-float plans (ARITH_DF) with block-quantised high
+                // words (1) instead of TwoSum additions (0); double plans
+                // (ARITH_F64): 2 = the radix-8 kernel's 64-bit fixed-point
+                // arithmetic (fft_fast.cuh, FX) on the power-of-two passes
 };
 
 // Launch one pass on `stream`.  Returns a cudaError_t value.

@@ -70,24 +70,28 @@ int double_arith() {
 }
 void set_double_arith(int a) { g_double_arith = a; }
 
-// Arithmetic of one double-precision plan.  Native FP64 issues at about 1/64
-// of the FP32 rate on this part, so large transforms run in float-float; a
-// transform of at most DARITH_AUTO_POINTS points costs no more than a launch
-// latency in FP64 and keeps full double rounding.  (Whether the float-float
-// radix-8 stages are block-quantised is Plan::quant, set with the arithmetic.)
-int plan_double_arith(const PlanDesc& d) {
+// Arithmetic of one double-precision plan.  The default (DARITH_AUTO) keeps
+// FFTW-class double answers: FP64 storage, the radix-8 kernel's 64-bit
+// fixed-point arithmetic on the power-of-two c2c passes (58 bits against the
+// tile's largest value, PassParams::quant = 2) and native FP64 on every other
+// pass.  DARITH_NATIVE runs every pass in FP64 on the general kernel.  The
+// float-float arithmetics (DARITH_DF TwoSum, DARITH_DFQ block-quantised
+// radix-8 butterflies) carry 48-49 bits and are opt-in: faster on this part,
+// whose FP64 pipe issues at about 1/70 of the FP32 rate, but narrower than
+// the reference's FFTW double.
+int plan_double_arith(const PlanDesc&) {
   const int m = double_arith();
-  if (m == DARITH_NATIVE) return ARITH_F64;
-  if (m == DARITH_DF || m == DARITH_DFQ) return ARITH_DF;
-  double pts = (double)d.howmany;
-  for (int t = 0; t < d.rnk_n; t++) pts *= (double)d.n[t];
-  return pts <= (double)DARITH_AUTO_POINTS ? ARITH_F64 : ARITH_DF;
+  return (m == DARITH_DF || m == DARITH_DFQ) ? ARITH_DF : ARITH_F64;
 }
 
-// Block-quantised float-float butterflies (fft_fast.cuh / fft_mixed.cuh, FQ)
-// for the plain c2c passes of a float-float plan: the double-arithmetic
-// modes DARITH_DFQ and DARITH_AUTO (above DARITH_AUTO_POINTS); DARITH_DF
-// keeps TwoSum additions everywhere.
+// PassParams::quant of every pass of a plan: 2 = 64-bit fixed point on the
+// radix-8 passes of a default double plan, 1 = block-quantised float-float
+// butterflies (DARITH_DFQ), 0 otherwise.
+static int plan_quant(const Plan* pl) {
+  if (pl->arith == ARITH_F64) return double_arith() == DARITH_AUTO ? 2 : 0;
+  if (pl->arith == ARITH_DF) return double_arith() == DARITH_DFQ ? 1 : 0;
+  return 0;
+}
 static void mark_quant(const Plan* pl, PassProgram* prog) {
   for (Pass& ps : prog->passes) ps.p.quant = pl->quant;
 }
@@ -150,10 +154,19 @@ Plan* make_plan(const PlanDesc& base, void* in, void* out) {
   Plan* pl = new Plan();
   pl->d = base;
   pl->arith = base.prec == 0 ? ARITH_F32 : plan_double_arith(base);
-  pl->quant = (pl->arith == ARITH_DF && (double_arith() == DARITH_DFQ || double_arith() == DARITH_AUTO)) ? 1 : 0;
+  pl->quant = plan_quant(pl);
+  // PFFT_BUFFERED_INPLACE (api/pfft.h:542; doc/tutorial.tex, "Preserving
+  // input data"): an out-of-place plan whose inputs and outputs are both
+  // stored in the input array, the output array being scratch.  Here the
+  // program is planned in place on the input array (plan-owned workspaces
+  // where a pass cannot run in place), so the output array is not touched.
+  // PFFT_PRESERVE_INPUT is what every out-of-place plan does anyway (no pass
+  // writes the input array), and PFFT_DESTROY_INPUT only permits
+  // overwriting it, which no program needs.
+  pl->buffered = (base.pfft_flags & F_BUFFERED_INPLACE) && in != out && in != nullptr;
   pl->in = in;
-  pl->out = out;
-  pl->inplace = (in == out) && in != nullptr;
+  pl->out = pl->buffered ? in : out;
+  pl->inplace = (pl->in == pl->out) && in != nullptr;
   if (!build_program(pl->d, pl->arith, pl->inplace, false, &pl->fwd)) {
     delete pl;
     return nullptr;
@@ -172,7 +185,7 @@ Plan* make_plan(const PlanDesc& base, void* in, void* out) {
   for (const Pass& ps : pl->fwd.passes) {
     cudaError_t e;
     bool ok = twiddle_table(ps.p.M, pl->arith, &e) && twiddle_table(ps.p.N, pl->arith, &e);
-    if (ok && pl->arith != ARITH_F64) fast_pass_tables(ps.p, pl->arith);  // radix-8 / mixed-radix tables
+    if (ok && (pl->arith != ARITH_F64 || pl->quant == 2)) fast_pass_tables(ps.p, pl->arith);  // radix-8 / mixed-radix tables
     if (!ok) {
       cuda_check(e, "twiddle table");
       destroy_plan(pl);
@@ -400,6 +413,7 @@ static int run_pipelined(Plan* pl, const PassProgram& prog, void* in, void* out,
 
 void execute_plan(Plan* pl, void* in, void* out, bool adjoint) {
   auto t0 = std::chrono::steady_clock::now();
+  if (pl->buffered) out = in;  // PFFT_BUFFERED_INPLACE: results go back to the array read
   if (adjoint && !pl->adj_built) {
     if (!build_program(pl->d, pl->arith, pl->inplace, true, &pl->adj)) {
       report("adjoint not available for this plan");

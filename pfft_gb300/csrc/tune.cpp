@@ -58,7 +58,7 @@ std::string key_of(const PassParams& p, int arith) {
   for (int b = 0; b < p.nb; b++) k << p.bext[b] << ":" << p.bsI[b] << ":" << p.bsO[b] << ",";
   k << ".f" << p.conj_in << p.conj_out << p.wmode << p.in_df << p.out_df << p.ashI.en << p.ashO.en;
   for (int b = 0; b < p.nb; b++) k << p.bshI[b].en << p.bshO[b].en;
-  if (p.quant) k << ".q1";
+  if (p.quant) k << ".q" << p.quant;
   return k.str();
 }
 

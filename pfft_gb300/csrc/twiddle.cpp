@@ -57,6 +57,13 @@ void packed_entry(long double c, long double s, float* h, float* l) {
   h[0] = rh; h[1] = rh; h[2] = -ih; h[3] = ih;
   l[0] = rl; l[1] = rl; l[2] = -il; l[3] = il;
 }
+// v * 2^61 rounded to an integer, split as hi * 2^32 + lo, lo in [-2^31, 2^31)
+void fx_split(long double v, int* hl) {
+  const long long x = llroundl(ldexpl(v, 61));
+  const long long hi = (x + (1ll << 31)) >> 32;
+  hl[0] = (int)hi;
+  hl[1] = (int)(x - hi * (1ll << 32));
+}
 }  // namespace
 
 const void* twiddle_table(int M, int arith, cudaError_t* err) {
@@ -64,9 +71,10 @@ const void* twiddle_table(int M, int arith, cudaError_t* err) {
   auto key = std::make_pair(M, arith);
   auto it = g_tables.find(key);
   if (it != g_tables.end()) return it->second;
-  const bool staged = arith == TW_F32_STG || arith == TW_DFP_FWD_STG || arith == TW_DFP_BWD_STG;
+  const bool fx = arith == TW_FX_FWD_STG || arith == TW_FX_BWD_STG;
+  const bool staged = arith == TW_F32_STG || arith == TW_DFP_FWD_STG || arith == TW_DFP_BWD_STG || fx;
   const bool packed = arith == TW_DFP_FWD || arith == TW_DFP_BWD || arith == TW_DFP_FWD_STG || arith == TW_DFP_BWD_STG;
-  const bool bwd = arith == TW_DFP_BWD || arith == TW_DFP_BWD_STG;
+  const bool bwd = arith == TW_DFP_BWD || arith == TW_DFP_BWD_STG || arith == TW_FX_BWD_STG;
   if (staged && (M < 16 || (M & (M - 1)))) {
     if (err) *err = cudaErrorInvalidValue;
     return nullptr;
@@ -87,8 +95,8 @@ const void* twiddle_table(int M, int arith, cudaError_t* err) {
   }
   const size_t n = expo.size();
   size_t bytes;
-  if (packed)
-    bytes = n * 32;
+  if (packed || fx)
+    bytes = n * (packed ? 32 : 24);
   else if (arith == ARITH_F32 || arith == TW_F32_STG)
     bytes = n * 8;
   else
@@ -98,7 +106,15 @@ const void* twiddle_table(int M, int arith, cudaError_t* err) {
     long double c, s;
     cis(expo[j], M, &c, &s);
     s = -s;  // forward direction
-    if (packed) {
+    if (fx) {
+      if (bwd) s = -s;
+      const long double v[3] = {c, s - c, c + s};
+      for (int q = 0; q < 3; q++) {
+        int hl[2];
+        fx_split(v[q], hl);
+        memcpy(&host[(q * n + j) * 8], hl, 8);
+      }
+    } else if (packed) {
       if (bwd) s = -s;
       float h[4], l[4];
       packed_entry(c, s, h, l);

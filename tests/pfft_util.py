@@ -85,8 +85,9 @@ def comm_for(req):
 
 class double_arith:
     """Context manager selecting the double API's arithmetic for the plans
-    created inside it: "double" keeps the default (by size), "double-df" forces
-    float-float, "double-f64" native FP64, "double-dfq" float-float with
+    created inside it: "double" keeps the default (64-bit fixed point on the
+    radix-8 passes, FP64 elsewhere), "double-f64" native FP64 everywhere,
+    "double-df" TwoSum float-float, "double-dfq" float-float with
     block-quantised radix-8 stages; "float" changes nothing."""
 
     MODES = {"double-df": 0, "double-f64": 1, "double-dfq": 3}
@@ -133,13 +134,17 @@ def gpu_run(req, x, prec="double", inplace=False, adjoint=False, torch=None, kee
     comm = comm_for(req)
     fn = getattr(L, pre + PLAN_NAME[req.kind])
     n, ni, no = pg.ints(req.n), pg.ints(req.ni), pg.ints(req.no)
+    # the _skipped planners take the per-axis skip flags after the block sizes
+    pre_args = (req.d, n, ni, no, req.howmany, None, None)
+    if req.skip is not None:
+        fn = getattr(L, pre + PLAN_NAME[req.kind] + "_skipped")
+        pre_args = pre_args + (pg.cints(req.skip),)
     with double_arith(prec):
         if req.kind == "r2r":
             kinds = pg.cints(req.kinds)
-            plan = fn(req.d, n, ni, no, req.howmany, None, None, a.data_ptr(), b.data_ptr(), comm, kinds, req.flags)
+            plan = fn(*pre_args, a.data_ptr(), b.data_ptr(), comm, kinds, req.flags)
         else:
-            plan = fn(req.d, n, ni, no, req.howmany, None, None, a.data_ptr(), b.data_ptr(), comm, req.sign,
-                      req.flags)
+            plan = fn(*pre_args, a.data_ptr(), b.data_ptr(), comm, req.sign, req.flags)
     if not plan:
         raise RuntimeError("planner returned NULL: %s" % (pg.last_error(),))
     try:

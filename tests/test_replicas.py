@@ -25,7 +25,7 @@ def test_reference_arm_two_ranks(pfft_lib):
     ob.build()
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2", "--master-addr",
            "127.0.0.1", "--master-port", str(_free_port()), os.path.join(ROOT, "bench.py"), "--impl", "reference",
-           "--gpus", "2", "--steps", "1", "--warmup", "3", "--ref-sample-n0", "4"]
+           "--gpus", "2", "--steps", "1", "--warmup", "3", "--ref-n", "32", "--no-scipy"]
     env = dict(os.environ, OMP_NUM_THREADS="1")
     out = subprocess.run(cmd, capture_output=True, text=True, timeout=300, cwd=ROOT, env=env)
     assert out.returncode == 0, out.stderr[-3000:]
