@@ -146,14 +146,18 @@ def cpu_input(n, seed=1):
     return np.random.default_rng(seed).uniform(-1.0, 1.0, 2 * int(np.prod(n)))
 
 
-def cpu_baseline(n=N3, threads=None, x=None):
+def cpu_baseline(n=N3, threads=None, x=None, keep=None):
     """Time the CPU oracle on one full forward execute of the workload (the
-    whole 512^3 complex128 transform, about 3 s on 16 cores)."""
+    whole 512^3 complex128 transform, about 3 s on 16 cores).  keep: a dict
+    that receives the oracle's output ("out"), the FP64 reference the GPU
+    results are compared with."""
     threads = threads or (os.cpu_count() or 1)
     x = cpu_input(n) if x is None else x
     t0 = time.perf_counter()
-    _oracle_forward(n, x, threads)
+    y = _oracle_forward(n, x, threads)
     dt = time.perf_counter() - t0
+    if keep is not None:
+        keep["out"] = y
     return {"value": algo_bytes(n) / dt / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
             "sample": "the full workload: one %s c2c complex128 forward, %.2f s" % ("x".join(map(str, n)), dt),
             "seconds": dt}
@@ -301,6 +305,234 @@ def measure_adjoint(L, pg, torch, reps=5):
         del x, y
         torch.cuda.empty_cache()
     return res
+
+
+
+# ---- the other configurations of the metric ---------------------------------------------
+DARITH = {"df": 0, "native": 1, "auto": 2, "dfq": 3}
+
+
+def rel_l2_np(a, b):
+    nb = float(np.linalg.norm(b))
+    return float(np.linalg.norm(a - b)) / (nb if nb > 0 else 1.0)
+
+
+def p_min(points, esz):
+    """Minimal HBM passes: ceil(log2 N / log2 M), M = 2^13 complex128 or 2^14
+    complex64 points staged by one CTA."""
+    return int(np.ceil(np.log2(points) / (13 if esz == 16 else 14)))
+
+
+def frac_key(peak):
+    return "frac_of_measured_peak" if peak[1] == "measured" else "frac_of_fallback_peak"
+
+
+def timed_stream(torch, stream, fn, reps, warm=2):
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def measure_arith_512(L, pg, torch, x_host, oracle_out, peak):
+    """The 512^3 complex128 forward in each double arithmetic and in complex64:
+    CUDA-event time, algorithmic GB/s, fraction of the HBM peak and the
+    forward relative L2 error against the FP64 oracle's output on the same
+    input (the double input rounded to float for complex64)."""
+    res = {}
+    n = N3
+    cnt = int(np.prod(n))
+    stream = torch.cuda.Stream()
+    comm = pg.procmesh(2)
+    old = L.pfft_gb300_get_double_arith()
+    labels = {"native": "f64 (native FP64 arithmetic on every pass, general kernel)",
+              "dfq": "f64 storage, float-float arithmetic with block-quantised radix-8 butterflies (48-49 bits; "
+                     "opt-in)",
+              "df": "f64 storage, TwoSum float-float arithmetic (48-49 bits; opt-in)",
+              "complex64": "f32 (the reference's single-precision API, pfftf_)"}
+    for name in ("native", "dfq", "df", "complex64"):
+        pre = "pfftf_" if name == "complex64" else "pfft_"
+        if name != "complex64":
+            L.pfft_gb300_set_double_arith(DARITH[name])
+        dt = torch.float32 if name == "complex64" else torch.float64
+        a = x_host.to(dt).cuda()
+        b = torch.empty_like(a)
+        flags = pg.PFFT_MEASURE if name == "native" else pg.PFFT_PATIENT
+        p = getattr(L, pre + "plan_dft_3d")(pg.ints(n), a.data_ptr(), b.data_ptr(), comm, pg.PFFT_FORWARD, flags)
+        L.pfft_gb300_set_double_arith(old)
+        if not p:
+            res[name] = {"error": "plan failed: %s" % (pg.last_error(),)}
+            continue
+        getattr(L, pre + "gb300_set_stream")(p, ctypes.c_void_p(stream.cuda_stream))
+        getattr(L, pre + "gb300_set_sync")(p, 0)
+        reps = 3 if name == "native" else 10
+        ms = timed_stream(torch, stream, lambda: getattr(L, pre + "execute")(p), reps)
+        esz = 8 if name == "complex64" else 16
+        B = p_min(cnt, esz) * 2 * cnt * esz
+        r = {"dtype": labels[name], "ms": ms, "gbs": B / (ms * 1e-3) / 1e9, "bytes": B,
+             frac_key(peak): B / (ms * 1e-3) / 1e9 / peak[0]}
+        if oracle_out is not None:
+            r["forward_rel_l2_vs_fp64_oracle"] = rel_l2_np(b.double().cpu().numpy(), oracle_out)
+        res[name] = r
+        getattr(L, pre + "destroy_plan")(p)
+        del a, b
+        torch.cuda.empty_cache()
+    return res
+
+
+def _alloc_words(L, pg, pre, kind, n, ni, no, flags, comm):
+    d = len(n)
+    a = [pg.ints([0] * d) for _ in range(4)]
+    ls = {"c2c": "local_size_many_dft", "r2c": "local_size_many_dft_r2c", "c2r": "local_size_many_dft_c2r",
+          "r2r": "local_size_many_r2r"}[kind]
+    alloc = getattr(L, pre + ls)(d, pg.ints(n), pg.ints(ni), pg.ints(no), 1, None, None, comm, flags, *a)
+    return alloc, [list(v) for v in a]
+
+
+def _plan(L, pg, pre, kind, n, ni, no, x, y, comm, sign, flags, kinds=None):
+    d = len(n)
+    pl = {"c2c": "plan_many_dft", "r2c": "plan_many_dft_r2c", "c2r": "plan_many_dft_c2r",
+          "r2r": "plan_many_r2r"}[kind]
+    last = pg.cints(kinds) if kind == "r2r" else sign
+    return getattr(L, pre + pl)(d, pg.ints(n), pg.ints(ni), pg.ints(no), 1, None, None, x.data_ptr(), y.data_ptr(),
+                                comm, last, flags)
+
+
+def measure_config(L, pg, torch, kind, n, prec, flags_f, flags_b, B, peak, ni=None, kinds=None, kinds_inv=None,
+                   norm=None, inplace=False, dist="uniform", reps=10):
+    """One configuration: the forward execute timed with CUDA events
+    (algorithmic bytes B per execute), then the inverse plan's round trip
+    error against the input (a size-independent check)."""
+    pre = "pfft_" if prec == "double" else "pfftf_"
+    rdt = torch.float64 if prec == "double" else torch.float32
+    comm = pg.procmesh(2)
+    ni = list(ni or n)
+    inv = {"c2c": "c2c", "r2c": "c2r", "r2r": "r2r"}[kind]
+    allocf, (lni, _, lno, _) = _alloc_words(L, pg, pre, kind, n, ni, n, flags_f, comm)
+    allocb, _ = _alloc_words(L, pg, pre, inv, n, n, ni, flags_b, comm)
+    words = 2 * max(allocf, allocb)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    x = torch.zeros(words, dtype=rdt, device="cuda")
+    cin = int(np.prod(lni)) * (2 if kind == "c2c" else 1)
+    if dist == "normal":
+        x[:cin].normal_(generator=g)
+    else:
+        x[:cin].uniform_(-1, 1, generator=g)
+    if kind == "r2c" and (flags_f & pg.PFFT_PADDED_R2C):
+        x[:cin].view(-1, lni[-1])[:, ni[-1]:] = 0
+    x0 = x.clone()
+    y = x if inplace else torch.zeros(words, dtype=rdt, device="cuda")
+    z = torch.zeros(words, dtype=rdt, device="cuda")
+    pf = _plan(L, pg, pre, kind, n, ni, n, x, y, comm, -1, flags_f | pg.PFFT_PATIENT, kinds)
+    if not pf:
+        return {"error": "plan failed: %s" % (pg.last_error(),)}
+    stream = torch.cuda.Stream()
+    getattr(L, pre + "gb300_set_stream")(pf, ctypes.c_void_p(stream.cuda_stream))
+    getattr(L, pre + "gb300_set_sync")(pf, 0)
+    if inplace:
+        # the input is restored before every step; events bracket the execute alone
+        times = []
+        for i in range(reps + 2):
+            with torch.cuda.stream(stream):
+                x.copy_(x0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            getattr(L, pre + "execute")(pf)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if i >= 2:
+                times.append(e0.elapsed_time(e1))
+        ms = float(np.median(times))
+        with torch.cuda.stream(stream):
+            x.copy_(x0)
+    else:
+        ms = timed_stream(torch, stream, lambda: getattr(L, pre + "execute")(pf), reps)
+    getattr(L, pre + "execute")(pf)
+    torch.cuda.synchronize()
+    dst = y if inplace else z
+    pb = _plan(L, pg, pre, inv, n, n, ni, y, dst, comm, 1, flags_b | pg.PFFT_MEASURE, kinds_inv)
+    rt = None
+    if pb:
+        getattr(L, pre + "execute")(pb)
+        torch.cuda.synchronize()
+        scale = norm if norm is not None else float(np.prod(n))
+        out = dst[:cin].double() / scale
+        ref = x0[:cin].double()
+        if kind == "r2c" and (flags_f & pg.PFFT_PADDED_R2C):
+            out = out.view(-1, lni[-1])[:, :ni[-1]]
+            ref = ref.view(-1, lni[-1])[:, :ni[-1]]
+        rt = float(torch.linalg.vector_norm(out - ref) / torch.linalg.vector_norm(ref))
+        getattr(L, pre + "destroy_plan")(pb)
+    getattr(L, pre + "destroy_plan")(pf)
+    gbs = B / (ms * 1e-3) / 1e9
+    r = {"ms": ms, "gbs": gbs, "bytes": B, frac_key(peak): gbs / peak[0], "roundtrip_rel_l2": rt,
+         "bound": 1e-12 if prec == "double" else 2e-6}
+    del x, y, z, x0
+    torch.cuda.empty_cache()
+    return r
+
+
+def measure_halo(L, pg, torch, peak, n=(256, 256, 256), w=2, reps=10):
+    """pfft_exchange of a 256^3 real float64 block with a halo of width 2 on
+    every face (periodic wrap, in place): CUDA-event time against the
+    algorithmic bytes, the block read once (134.2 MB) and the box written once
+    (140.6 MB); and the reduce, its adjoint, on the same bytes."""
+    comm = pg.procmesh(2)
+    box = [m + 2 * w for m in n]
+    buf = torch.zeros(int(np.prod(box)), dtype=torch.float64, device="cuda")
+    buf[: int(np.prod(n))].uniform_(-1, 1)
+    p = L.pfft_plan_rgc_3d(pg.ints(n), pg.ints([w] * 3), pg.ints([w] * 3), buf.data_ptr(), comm, 0)
+    if not p:
+        return {"error": "ghost plan failed"}
+    stream = torch.cuda.Stream()
+    L.pfft_gb300_gc_set_stream(p, ctypes.c_void_p(stream.cuda_stream))
+    B = int(np.prod(n)) * 8 + int(np.prod(box)) * 8
+    res = {"workload": "256^3 float64 real block, halo 2 on every face, periodic wrap, in place"}
+    for op in ("exchange", "reduce"):
+        fn = getattr(L, "pfft_" + op)
+        ms = timed_stream(torch, stream, lambda: fn(p), reps)
+        gbs = B / (ms * 1e-3) / 1e9
+        res[op] = {"ms": ms, "gbs": gbs, "bytes": B, frac_key(peak): gbs / peak[0]}
+    L.pfft_destroy_gcplan(p)
+    del buf
+    torch.cuda.empty_cache()
+    return res
+
+
+def measure_configs(L, pg, torch, peak):
+    """Every configuration of the metric besides the 512^3 headline (each a
+    forward execute with the default arithmetic; algorithmic bytes
+    B = in + out + 2 (P_min - 1) work)."""
+    TO, TI, PAD = pg.PFFT_TRANSPOSED_OUT, pg.PFFT_TRANSPOSED_IN, pg.PFFT_PADDED_R2C
+    c = {}
+    c["c2c_64cube_c128"] = measure_config(L, pg, torch, "c2c", (64, 64, 64), "double", 0, 0,
+                                          2 * 2 * 64 ** 3 * 16, peak)
+    n256 = (256, 256, 256)
+    for prec, esz in (("double", 8), ("float", 4)):
+        tag = "f64" if prec == "double" else "f32"
+        rin = 256 * 256 * 258 * esz
+        cout = 256 * 256 * 129 * 2 * esz
+        c["r2c_256cube_%s_padded_transposed_inplace" % tag] = measure_config(
+            L, pg, torch, "r2c", n256, prec, PAD | TO, PAD | TI, rin + cout + 2 * cout, peak, inplace=True,
+            dist="normal")
+        rb = 256 ** 3 * esz
+        c["redft10_256cube_%s" % tag] = measure_config(
+            L, pg, torch, "r2r", n256, prec, 0, 0, 4 * rb, peak, kinds=[pg.PFFT_REDFT10] * 3,
+            kinds_inv=[pg.PFFT_REDFT01] * 3, norm=float((2 * 256) ** 3), dist="normal")
+    c["ousam_r2c_f32_128to256"] = measure_config(L, pg, torch, "r2c", n256, "float", 0, 0, 211 * 10 ** 6, peak,
+                                                 ni=(128, 128, 128), dist="normal")
+    c["c2c_1024cube_c64"] = measure_config(L, pg, torch, "c2c", (1024, 1024, 1024), "float", 0, 0,
+                                           3 * 2 * 1024 ** 3 * 8, peak, reps=5)
+    c["c2c_64pow4_c128"] = measure_config(L, pg, torch, "c2c", (64, 64, 64, 64), "double", 0, 0,
+                                          2 * 2 * 64 ** 4 * 16, peak)
+    c["halo_256cube_w2_f64"] = measure_halo(L, pg, torch, peak)
+    return c
 
 
 def dist_setup(args):
@@ -508,21 +740,42 @@ def main():
                     "bound": 1e-12 if args.prec == "double" else 2e-6}
         getattr(L, pre + "destroy_plan")(pb)
     del c
+    # the forward output, for the comparison with the FP64 oracle on the same input
+    full = (n == N3 and rank == 0 and not args.no_cpu_baseline)
+    fwd_host = b.double().cpu().numpy() if full else None
     getattr(L, pre + "destroy_plan")(plan)
     del a, b
     torch.cuda.empty_cache()
 
-    # ---- the metric's other two parts: batched vs loop, adjoint cost (untimed by the step clock) ----
+    # ---- CPU baselines on the same workload (rank 0), and the FP64 oracle's output ----
+    cpu = {}
+    oracle_keep = {}
+    if full:
+        xb = host.double().numpy()
+        cpu["cpu_baseline"] = cpu_baseline(N3, x=xb, keep=oracle_keep)
+        if not args.no_scipy:
+            cpu["scipy_baseline"] = scipy_baseline(N3, x=xb)
+        if accuracy is not None:
+            accuracy["forward_rel_l2_vs_fp64_oracle"] = rel_l2_np(fwd_host, oracle_keep["out"])
+        del fwd_host
+
+    # ---- the metric's other parts: batched vs loop, adjoint cost, every arithmetic at 512^3,
+    # ---- the other configurations (outside the step's timed region) ----
     extra = {}
+    peak = measured_peak()
     if not args.no_extras:
         extra["batched_vs_loop"] = {pr: measure_batched(L, pg, torch, pr, tune=not args.no_tune)
                                     for pr in ("double", "float")}
         extra["adjoint_cost"] = measure_adjoint(L, pg, torch)
+        if n == N3 and args.prec == "double":
+            extra["arith_512"] = measure_arith_512(L, pg, torch, host, oracle_keep.get("out"), peak)
+        extra["configs"] = measure_configs(L, pg, torch, peak)
+    oracle_keep.clear()
 
     pts = int(np.prod(n))
     pmin = int(np.ceil(np.log2(pts) / (13 if esz == 16 else 14)))  # minimal HBM passes
     B = pmin * 2 * pts * esz
-    peak, peak_kind = measured_peak()
+    peak, peak_kind = peak
     value = world * B / (ms_max * 1e-3) / 1e9
     # dominant kernel: the pass with the largest share of the step
     k = int(np.argmax(pass_ms)) if pass_ms else 0
@@ -535,8 +788,12 @@ def main():
         "metric": "3D FFT HBM GB/s & %roofline, 5N*log2N GFLOP/s; batched vs loop; adjoint cost",
         "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": {0: "f32", 1: "f64", 2: "f64 storage, float-float arithmetic" +
-                  (" (block-quantised radix-8 stages)" if dmode in (2, 3) else " (TwoSum)")}[plan_arith],
+        "dtype": {0: "f32",
+                  1: ("f64 storage, int64 block-fixed-point arithmetic on the radix-8 passes (58 bits against the "
+                      "tile maximum; measured no less accurate than native FP64), FP64 elsewhere")
+                  if dmode == 2 else "f64 (native FP64 arithmetic)",
+                  2: "f64 storage, float-float arithmetic" +
+                  (" (block-quantised radix-8 stages)" if dmode == 3 else " (TwoSum)")}[plan_arith],
         "accuracy": accuracy,
         "data": "synthetic uniform[-1,1) seed 1+rank",
         "config": {"workload": "pfft_execute c2c %s %s forward, 1x1 procmesh, out-of-place, "
@@ -561,11 +818,7 @@ def main():
         "clocks": clk,
     }
     line.update(extra)
-    if not args.no_cpu_baseline:
-        xb = cpu_input(N3)
-        line["cpu_baseline"] = cpu_baseline(N3, x=xb)
-        if not args.no_scipy:
-            line["scipy_baseline"] = scipy_baseline(N3, x=xb)
+    line.update(cpu)
     print(json.dumps(line), flush=True)
 
 

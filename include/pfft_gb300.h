@@ -45,6 +45,12 @@ int pfft_gb300_set_graph(pfft_plan plan, int graph);
 int pfftf_gb300_set_graph(pfftf_plan plan, int graph);
 int pfft_gb300_set_pipeline(pfft_plan plan, int pipeline);
 int pfftf_gb300_set_pipeline(pfftf_plan plan, int pipeline);
+
+/* The CUDA stream (cudaStream_t) of a ghost-cell plan's exchange and reduce
+ * (default: the legacy default stream).  Both stay synchronous: they return
+ * once their work on that stream is done.  Returns 0, or -1 for a NULL plan. */
+int pfft_gb300_gc_set_stream(pfft_gcplan plan, void *stream);
+int pfftf_gb300_gc_set_stream(pfftf_gcplan plan, void *stream);
 /* Executes (both precisions) that went through the host-array pipeline so far
  * in this process. */
 long long pfft_gb300_pipelined_executes(void);

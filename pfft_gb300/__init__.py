@@ -140,6 +140,8 @@ def _declare(L):
         for nm in ("exchange", "reduce", "destroy_gcplan"):
             f(nm).restype = None
             f(nm).argtypes = [c_void_p]
+        f("gb300_gc_set_stream").restype = ctypes.c_int
+        f("gb300_gc_set_stream").argtypes = [c_void_p, c_void_p]
         for nm in ("alloc_real", "alloc_complex", "malloc"):
             f(nm).restype = c_void_p
             f(nm).argtypes = [ctypes.c_size_t]

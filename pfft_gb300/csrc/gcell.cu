@@ -10,11 +10,26 @@
 // cells that are its periodic images, then the box is truncated back to the
 // compact block and the rest of the buffer is zeroed.
 //
-// Both operations are in place on the user's buffer.  The box overlaps the
-// block it is built from, so the block (exchange) or the box (reduce) is first
-// copied into plan-owned scratch memory and one gather / scatter-add kernel
-// writes the result.
+// Both operations are in place on the user's buffer, in one sweep over the
+// data, as the reference pads in place from the back
+// (pad_array_with_zeros_outside_3d, gcells_plan.c:424-455) before its halo
+// messages:
+//   exchange  1. k_gc_move (expand): every block row moves to its interior
+//                position in the box, rows taken from the back in chunks;
+//             2. k_gc_fill: every ghost cell copies its interior image.
+//   reduce    1. k_gc_fold: every block cell with ghost images sums them,
+//                in place at its interior position;
+//             2. k_gc_move (compact): interior rows move back to the compact
+//                block, chunks taken from the front; the rest is zeroed.
+// A chunk's rows are staged in shared memory, so a chunk may overwrite its
+// own source; a chunk writes only after every earlier chunk (taken by an
+// atomic ticket, hence already running) whose source rows its writes cover
+// has read them (per-chunk flags, bounded waits with an error word).  Rows
+// longer than the staging area (more than 4096 doubles or 8192 floats) fall
+// back to a copy of the data in plan scratch memory and a gather /
+// scatter-add kernel.
 #include <stdio.h>
+#include <algorithm>
 #include <string.h>
 #include <chrono>
 #include "../../include/pfft.h"
@@ -78,13 +93,188 @@ __global__ void k_gc_reduce(const T* __restrict__ src, T* __restrict__ blk, GcDi
   }
 }
 
+// ---- single-sweep in-place kernels ------------------------------------------------
+constexpr int GC_THREADS = 256;
+constexpr int GC_STAGE_BYTES = 32 * 1024;  // staging area of a chunk (static shared memory)
+constexpr int GC_MAX_ROWS = 1024;          // rows per chunk (row-start table)
+
+struct GcMove {
+  long long rows;        // block rows (n0 * n1)
+  long long n1;          // block extent of axis 1
+  long long RS, RB;      // scalars per block row (n2 * tuple) and per box row (ng2 * tuple)
+  long long gb0, gb1, ng1;
+  long long off2;        // gc_below[2] * tuple: start of the interior in a box row
+  long long R;           // rows per chunk
+  long long nchunks;
+  unsigned* ticket;
+  unsigned* flags;       // one per chunk: the epoch once the chunk's rows are read
+  int* err;
+  unsigned epoch;
+  unsigned rs_magic;     // 0xFFFFFFFF / RS + 1 (RS > 1): f / RS = umulhi(f, rs_magic) for f, RS < 2^16
+  long long spin_limit;
+};
+
+__device__ __forceinline__ long long gc_box_start(const GcMove& m, long long row) {
+  const long long j0 = row / m.n1, j1 = row - j0 * m.n1;
+  return ((j0 + m.gb0) * m.ng1 + j1 + m.gb1) * m.RB + m.off2;
+}
+
+// EXPAND: block rows -> interior box rows, chunks from the back; otherwise
+// interior box rows -> block rows, chunks from the front
+template <class T, bool EXPAND>
+__global__ void __launch_bounds__(GC_THREADS) k_gc_move(T* __restrict__ data, const GcMove m) {
+  __shared__ __align__(16) unsigned char stage_raw[GC_STAGE_BYTES];
+  __shared__ long long boxrow[GC_MAX_ROWS];
+  __shared__ long long s_chunk;
+  T* stage = (T*)stage_raw;
+  const int tid = threadIdx.x;
+  for (;;) {
+    if (tid == 0) s_chunk = (long long)atomicAdd(m.ticket, 1u);
+    __syncthreads();
+    const long long c = s_chunk;
+    if (c >= m.nchunks) break;
+    long long r_lo, r_hi;
+    if (EXPAND) {
+      r_hi = m.rows - c * m.R;
+      r_lo = r_hi - m.R > 0 ? r_hi - m.R : 0;
+    } else {
+      r_lo = c * m.R;
+      r_hi = r_lo + m.R < m.rows ? r_lo + m.R : m.rows;
+    }
+    const int nr = (int)(r_hi - r_lo);
+    for (int q = tid; q < nr; q += GC_THREADS) boxrow[q] = gc_box_start(m, r_lo + q);
+    __syncthreads();
+    const unsigned nsc = (unsigned)(nr * m.RS);
+    // read the chunk's rows
+    if (EXPAND) {
+      const T* src = data + r_lo * m.RS;  // block rows are contiguous
+      for (unsigned f = tid; f < nsc; f += GC_THREADS) stage[f] = src[f];
+    } else {
+      for (unsigned f = tid; f < nsc; f += GC_THREADS) {
+        const unsigned q = m.RS == 1 ? f : __umulhi(f, m.rs_magic);
+        stage[f] = data[boxrow[q] + (f - q * (unsigned)m.RS)];
+      }
+    }
+    __syncthreads();
+    if (tid == 0) {
+      __threadfence();
+      atomicExch(m.flags + c, m.epoch);
+    }
+    // earlier chunks whose source rows this chunk's writes cover
+    long long w_lo = c, w_hi = c - 1;
+    if (EXPAND) {
+      const long long whi = boxrow[nr - 1] + m.RS - 1;  // last scalar written
+      long long rmax = whi / m.RS;
+      if (rmax > m.rows - 1) rmax = m.rows - 1;
+      if (rmax >= r_hi) w_lo = (m.rows - 1 - rmax) / m.R;
+    } else if (r_lo > 0) {
+      // first row whose box source ends past this chunk's first written scalar
+      const long long wlo = r_lo * m.RS;
+      long long a = 0, b = r_lo;
+      while (a < b) {
+        const long long mid = (a + b) / 2;
+        if (gc_box_start(m, mid) + m.RS > wlo)
+          b = mid;
+        else
+          a = mid + 1;
+      }
+      if (a < r_lo) w_lo = a / m.R;
+    }
+    for (long long q = w_lo + tid; q <= w_hi; q += GC_THREADS) {
+      const volatile unsigned* fl = m.flags + q;
+      long long it = 0;
+      while (*fl != m.epoch) {
+        if (++it > m.spin_limit) {
+          atomicExch(m.err, 1);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    __syncthreads();
+    // write
+    if (EXPAND) {
+      for (unsigned f = tid; f < nsc; f += GC_THREADS) {
+        const unsigned q = m.RS == 1 ? f : __umulhi(f, m.rs_magic);
+        data[boxrow[q] + (f - q * (unsigned)m.RS)] = stage[f];
+      }
+    } else {
+      T* dst = data + r_lo * m.RS;
+      for (unsigned f = tid; f < nsc; f += GC_THREADS) dst[f] = stage[f];
+    }
+    __syncthreads();
+  }
+}
+
+__device__ __forceinline__ long long gc_wrap(long long k, long long n) {
+  long long j = k % n;
+  return j < 0 ? j + n : j;
+}
+
+// every ghost cell of the box <- its interior image (one warp per box row)
+template <class T>
+__global__ void __launch_bounds__(GC_THREADS) k_gc_fill(T* __restrict__ data, GcDims g, long long nrows) {
+  const int lane = threadIdx.x & 31;
+  const long long warps = (long long)gridDim.x * (GC_THREADS / 32);
+  const long long tu = g.tuple, RB = g.ng[2] * tu, gb2t = g.gb[2] * tu, endt = (g.gb[2] + g.n[2]) * tu;
+  for (long long b = (long long)blockIdx.x * (GC_THREADS / 32) + (threadIdx.x >> 5); b < nrows; b += warps) {
+    const long long k0 = b / g.ng[1], k1 = b - k0 * g.ng[1];
+    const bool interior = k0 >= g.gb[0] && k0 < g.gb[0] + g.n[0] && k1 >= g.gb[1] && k1 < g.gb[1] + g.n[1];
+    const long long j0 = gc_wrap(k0 - g.gb[0], g.n[0]), j1 = gc_wrap(k1 - g.gb[1], g.n[1]);
+    const T* src = data + ((j0 + g.gb[0]) * g.ng[1] + j1 + g.gb[1]) * RB;
+    T* dst = data + b * RB;
+    // interior rows: the cells before and after the interior; ghost rows: all
+    const long long cnt = interior ? RB - (endt - gb2t) : RB;
+    for (long long s = lane; s < cnt; s += 32) {
+      const long long t = (interior && s >= gb2t) ? s + (endt - gb2t) : s;  // scalar of the box row
+      const long long k2 = t / tu, h = t - k2 * tu;
+      dst[t] = src[(gc_wrap(k2 - g.gb[2], g.n[2]) + g.gb[2]) * tu + h];
+    }
+  }
+}
+
+// every block cell with more than one image <- the sum of its images
+// (k0, k1, k2 ascending), written at its interior position (one warp per
+// block row)
+template <class T>
+__global__ void __launch_bounds__(GC_THREADS) k_gc_fold(T* __restrict__ data, GcDims g, long long nrows) {
+  const int lane = threadIdx.x & 31;
+  const long long warps = (long long)gridDim.x * (GC_THREADS / 32);
+  const long long tu = g.tuple;
+  for (long long r = (long long)blockIdx.x * (GC_THREADS / 32) + (threadIdx.x >> 5); r < nrows; r += warps) {
+    const long long j0 = r / g.n[1], j1 = r - j0 * g.n[1];
+    const long long s0 = (j0 + g.gb[0]) % g.n[0], s1 = (j1 + g.gb[1]) % g.n[1];
+    const bool many01 = s0 + g.n[0] < g.ng[0] || s1 + g.n[1] < g.ng[1];
+    for (long long j2 = lane; j2 < g.n[2]; j2 += 32) {
+      const long long s2 = (j2 + g.gb[2]) % g.n[2];
+      if (!many01 && s2 + g.n[2] >= g.ng[2]) continue;  // a single image: nothing to add
+      const long long at = (((j0 + g.gb[0]) * g.ng[1] + j1 + g.gb[1]) * g.ng[2] + j2 + g.gb[2]) * tu;
+      for (long long h = 0; h < tu; h++) {
+        T acc = 0;
+        for (long long k0 = s0; k0 < g.ng[0]; k0 += g.n[0])
+          for (long long k1 = s1; k1 < g.ng[1]; k1 += g.n[1])
+            for (long long k2 = s2; k2 < g.ng[2]; k2 += g.n[2])
+              acc += data[((k0 * g.ng[1] + k1) * g.ng[2] + k2) * tu + h];
+        data[at + h] = acc;
+      }
+    }
+  }
+}
+
 struct GcPlan {
   int prec;  // 0 float, 1 double
   void* data;
   GcDims g;
   long long ncomp, nbox;  // cells
-  void* scratch = nullptr;
+  void* scratch = nullptr;  // only rows longer than the staging area (copy + gather path)
   size_t scratch_bytes = 0;
+  bool single_sweep = true;
+  long long R = 1, nchunks = 0;  // rows per chunk, chunks of the in-place moves
+  unsigned* ctl = nullptr;       // device: ticket, error word, one flag per chunk
+  int* h_err = nullptr;          // pinned copy of the error word
+  unsigned epoch = 0;
+  int sms = 1;
   cudaStream_t stream = 0;
   // timers (gcell/gctimer.c layout: iter, whole, pad_zeros, exchange)
   double texg[4] = {0, 0, 0, 0};
@@ -106,6 +296,14 @@ bool dev_ptr(const void* p) {
     return false;
   }
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+void gc_free(GcPlan* p) {
+  if (!p) return;
+  if (p->scratch) cudaFree(p->scratch);
+  if (p->ctl) cudaFree(p->ctl);
+  if (p->h_err) cudaFreeHost(p->h_err);
+  delete p;
 }
 
 GcPlan* make_gc(int prec, int rnk, const INT* n_user, INT howmany, const INT* gcb_user, const INT* gca_user,
@@ -152,7 +350,7 @@ GcPlan* make_gc(int prec, int rnk, const INT* n_user, INT howmany, const INT* gc
   p->nbox = 1;
   for (int t = 0; t < 3; t++) {
     if (pn[t] <= 0 || pgb[t] < 0 || pga[t] < 0) {
-      delete p;
+      gc_free(p);
       return nullptr;
     }
     p->g.n[t] = pn[t];
@@ -162,20 +360,85 @@ GcPlan* make_gc(int prec, int rnk, const INT* n_user, INT howmany, const INT* gc
     p->nbox *= p->g.ng[t];
   }
   p->g.tuple = tuple;
-  p->scratch_bytes = (size_t)p->nbox * tuple * esz(p);
-  if (cuda_check(cudaMalloc(&p->scratch, p->scratch_bytes), "ghost-cell scratch")) {
-    delete p;
-    return nullptr;
+  const long long RS = p->g.n[2] * tuple;
+  const long long cap = GC_STAGE_BYTES / (long long)esz(p);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, dev);
+  if (p->sms < 1) p->sms = 1;
+  if (RS <= cap) {
+    p->R = std::min<long long>(GC_MAX_ROWS, cap / RS);
+    const long long rows = p->g.n[0] * p->g.n[1];
+    p->nchunks = (rows + p->R - 1) / p->R;
+    if (cuda_check(cudaMalloc(&p->ctl, sizeof(unsigned) * (size_t)(2 + p->nchunks)), "ghost-cell flags") ||
+        cuda_check(cudaMemset(p->ctl, 0, sizeof(unsigned) * (size_t)(2 + p->nchunks)), "ghost-cell flags") ||
+        cuda_check(cudaMallocHost(&p->h_err, sizeof(int)), "ghost-cell error word")) {
+      gc_free(p);
+      return nullptr;
+    }
+  } else {
+    p->single_sweep = false;
+    p->scratch_bytes = (size_t)p->nbox * tuple * esz(p);
+    if (cuda_check(cudaMalloc(&p->scratch, p->scratch_bytes), "ghost-cell scratch")) {
+      gc_free(p);
+      return nullptr;
+    }
   }
   return p;
 }
 
+GcMove gc_move_args(GcPlan* p) {
+  GcMove m;
+  m.rows = p->g.n[0] * p->g.n[1];
+  m.n1 = p->g.n[1];
+  m.RS = p->g.n[2] * p->g.tuple;
+  m.RB = p->g.ng[2] * p->g.tuple;
+  m.gb0 = p->g.gb[0];
+  m.gb1 = p->g.gb[1];
+  m.ng1 = p->g.ng[1];
+  m.off2 = p->g.gb[2] * p->g.tuple;
+  m.R = p->R;
+  m.nchunks = p->nchunks;
+  m.ticket = p->ctl;
+  m.err = (int*)(p->ctl + 1);
+  m.flags = p->ctl + 2;
+  if (++p->epoch == 0) p->epoch = 1;  // flags start at 0, so epoch 0 is never used
+  m.epoch = p->epoch;
+  m.rs_magic = m.RS > 1 ? (unsigned)(0xFFFFFFFFull / (unsigned long long)m.RS + 1) : 0u;
+  m.spin_limit = 20000000;  // about 2 s of 64 ns naps
+  return m;
+}
+
+template <class T, bool EXPAND>
+int gc_move(GcPlan* p, void* data) {
+  cudaError_t e = cudaMemsetAsync(p->ctl, 0, 2 * sizeof(unsigned), p->stream);  // ticket, error word
+  if (e != cudaSuccess) return (int)e;
+  const GcMove m = gc_move_args(p);
+  const long long grid = std::min<long long>(m.nchunks, (long long)p->sms * 4);
+  if (grid > 0) k_gc_move<T, EXPAND><<<(unsigned)grid, GC_THREADS, 0, p->stream>>>((T*)data, m);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return (int)e;
+  return (int)cudaMemcpyAsync(p->h_err, p->ctl + 1, sizeof(int), cudaMemcpyDeviceToHost, p->stream);
+}
+
+int gc_rows_grid(const GcPlan* p, long long rows) {
+  const long long want = (rows + (GC_THREADS / 32) - 1) / (GC_THREADS / 32);
+  return (int)std::max(1LL, std::min<long long>(want, (long long)p->sms * 8));
+}
+
 template <class T>
 int gc_exchange_t(GcPlan* p, void* data) {
-  size_t cb = (size_t)p->ncomp * p->g.tuple * sizeof(T);
-  cudaError_t e = cudaMemcpyAsync(p->scratch, data, cb, cudaMemcpyDeviceToDevice, p->stream);
-  if (e != cudaSuccess) return (int)e;
-  k_gc_gather<T><<<launch_grid(p->nbox), 256, 0, p->stream>>>((const T*)p->scratch, (T*)data, p->g, p->nbox);
+  if (!p->single_sweep) {
+    size_t cb = (size_t)p->ncomp * p->g.tuple * sizeof(T);
+    cudaError_t e = cudaMemcpyAsync(p->scratch, data, cb, cudaMemcpyDeviceToDevice, p->stream);
+    if (e != cudaSuccess) return (int)e;
+    k_gc_gather<T><<<launch_grid(p->nbox), 256, 0, p->stream>>>((const T*)p->scratch, (T*)data, p->g, p->nbox);
+    return (int)cudaGetLastError();
+  }
+  int rc = gc_move<T, true>(p, data);
+  if (rc) return rc;
+  const long long rows = p->g.ng[0] * p->g.ng[1];
+  k_gc_fill<T><<<gc_rows_grid(p, rows), GC_THREADS, 0, p->stream>>>((T*)data, p->g, rows);
   return (int)cudaGetLastError();
 }
 
@@ -183,9 +446,19 @@ template <class T>
 int gc_reduce_t(GcPlan* p, void* data) {
   size_t bb = (size_t)p->nbox * p->g.tuple * sizeof(T);
   size_t cb = (size_t)p->ncomp * p->g.tuple * sizeof(T);
-  cudaError_t e = cudaMemcpyAsync(p->scratch, data, bb, cudaMemcpyDeviceToDevice, p->stream);
-  if (e != cudaSuccess) return (int)e;
-  k_gc_reduce<T><<<launch_grid(p->ncomp), 256, 0, p->stream>>>((const T*)p->scratch, (T*)data, p->g, p->ncomp);
+  cudaError_t e;
+  if (!p->single_sweep) {
+    e = cudaMemcpyAsync(p->scratch, data, bb, cudaMemcpyDeviceToDevice, p->stream);
+    if (e != cudaSuccess) return (int)e;
+    k_gc_reduce<T><<<launch_grid(p->ncomp), 256, 0, p->stream>>>((const T*)p->scratch, (T*)data, p->g, p->ncomp);
+  } else {
+    const long long rows = p->g.n[0] * p->g.n[1];
+    k_gc_fold<T><<<gc_rows_grid(p, rows), GC_THREADS, 0, p->stream>>>((T*)data, p->g, rows);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return (int)e;
+    int rc = gc_move<T, false>(p, data);
+    if (rc) return rc;
+  }
   e = cudaGetLastError();
   if (e != cudaSuccess) return (int)e;
   if (bb > cb) e = cudaMemsetAsync((char*)data + cb, 0, bb - cb, p->stream);
@@ -217,6 +490,11 @@ void gc_run(GcPlan* p, bool reduce) {
   if (tmp) cudaFree(tmp);
   if (rc) {
     cuda_check((cudaError_t)rc, reduce ? "reduce" : "exchange");
+    return;
+  }
+  if (p->single_sweep && *p->h_err) {
+    report("%s: a chunk's wait for the rows it overwrites timed out; the result is not valid",
+           reduce ? "reduce" : "exchange");
     return;
   }
   double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -304,8 +582,7 @@ struct pfftf_gctimer_s {
   }                                                                                                        \
   void PX##destroy_gcplan(PX##gcplan ths) {                                                                \
     if (!ths) return;                                                                                      \
-    if (ths->p->scratch) cudaFree(ths->p->scratch);                                                        \
-    delete ths->p;                                                                                         \
+    gc_free(ths->p);                                                                                       \
     delete ths;                                                                                            \
   }                                                                                                        \
   int PX##gb300_gc_set_stream(PX##gcplan ths, void* stream) {                                              \

@@ -78,6 +78,13 @@ static const rt_case CASES[] = {
     {"simple_check_ousam_c2r", C2R, 3, {29, 27, 31}, {16, 16, 16}, 0, 0, 0, 0, {0}, {0}, 0},
     {"simple_check_ousam_r2r", R2R, 3, {29, 27, 31}, {16, 16, 16}, 0, 0, 0, 0, K3F, K3B, 0},
     {"simple_check_ousam_r2r_transposed", R2R, 3, {29, 27, 31}, {16, 16, 16}, TO, TI, 0, 0, K3F, K3B, 0},
+    /* the same checks (golden data, 1e-12 bound) at sizes beyond the
+     * reference's suite, where the double API's default arithmetic runs the
+     * radix-8 kernel's 64-bit fixed point on every power-of-two axis */
+    {"large_check_c2c_128", C2C, 3, {128, 128, 128}, {0}, 0, 0, 0, 0, {0}, {0}, 0},
+    {"large_check_c2c_256_transposed", C2C, 3, {256, 256, 256}, {0}, TO, TI, 0, 0, {0}, {0}, 0},
+    {"large_check_c2c_512x256x128", C2C, 3, {512, 256, 128}, {0}, 0, 0, 0, 0, {0}, {0}, 0},
+    {"large_check_r2c_256_padded_transposed", R2C, 3, {256, 256, 256}, {0}, PAD | TO, PAD | TI, 0, 0, {0}, {0}, 0},
 };
 
 /* logical length of a real-to-real transform (the normalisation factor) */

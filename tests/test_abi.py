@@ -36,3 +36,23 @@ def test_library_exports_all_declared_symbols(pfft_lib):
 def test_library_has_no_torch_dependency(pfft_lib):
     out = subprocess.run(["ldd", pg.LIBPATH], capture_output=True, text=True).stdout
     assert "torch" not in out and "c10" not in out
+
+
+def test_noalloc_buffer_rule(pfft_lib):
+    """The buffer check of the allocation-free exchange (no GPU needed):
+    managed memory and device memory of the current device are accepted; a
+    device pointer of another GPU is refused with cudaErrorInvalidDevice
+    (101) and host memory with cudaErrorInvalidValue (1), before anything is
+    queued."""
+    import ctypes
+    f = pfft_lib.pg_noalloc_buffer_check
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    unregistered, host, device, managed = 0, 1, 2, 3  # cudaMemoryType
+    assert f(device, 0, 0) == 0
+    assert f(device, 3, 3) == 0
+    assert f(managed, 0, 1) == 0
+    assert f(device, 1, 0) == 101
+    assert f(device, 0, 2) == 101
+    assert f(host, 0, 0) == 1
+    assert f(unregistered, 0, 0) == 1

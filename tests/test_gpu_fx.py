@@ -1,0 +1,94 @@
+"""The double API's default arithmetic on the radix-8 kernel: 64-bit block
+fixed point (fft_fast.cuh, FX), against the FP64 oracle and against native
+FP64 on the same inputs (GPU, through the C-ABI).
+
+FX converts each tile's doubles to int64 mantissas on the tile's common grid
+(58 bits below the tile's largest exponent), adds exactly and multiplies by
+64-bit twiddles; it must be at least as accurate as native FP64 arithmetic
+(the reference computes in FFTW double) on every length, direction and
+layout, exactly invariant under power-of-two scaling of the input (the grid
+follows the exponent), and must turn a tile holding an infinity or NaN into
+NaN instead of garbage.
+"""
+import numpy as np
+import pytest
+
+import pfft_gb300 as pg
+from tests.pfft_util import Req, gpu_run, oracle_run, random_input, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(16, 16, 16), (8, 32, 64), (4, 8, 128), (2, 4, 256), (2, 2, 512), (2, 1024, 2), (2, 2048, 1),
+          (4096, 2, 1), (32, 64, 128)]
+
+
+@pytest.mark.parametrize("sign", [-1, 1])
+@pytest.mark.parametrize("flags", [0, pg.PFFT_TRANSPOSED_OUT])
+@pytest.mark.parametrize("n", SHAPES)
+def test_fx_no_less_accurate_than_native_fp64(cuda, pfft_lib, n, flags, sign):
+    req = Req("c2c", n, sign=sign, flags=flags)
+    rng = np.random.default_rng(sum(n) + sign + flags)
+    x = random_input(req, rng)
+    ref = oracle_run(req, x)
+    fx = gpu_run(req, x, prec="double")
+    nat = gpu_run(req, x, prec="double-f64")
+    e_fx, e_nat = rel_l2(fx, ref), rel_l2(nat, ref)
+    assert e_fx <= 1e-15, e_fx
+    assert e_fx <= 1.25 * e_nat + 1e-17, (e_fx, e_nat)
+
+
+@pytest.mark.parametrize("dist", ["spread", "spike", "one_line"])
+def test_fx_dynamic_range(cuda, pfft_lib, dist):
+    """Values spread over 2^+-40, a single large value among small ones, and
+    one line a million times larger than the others: FX's error, relative to
+    the result's norm, stays within native FP64's."""
+    req = Req("c2c", (64, 32, 128))
+    rng = np.random.default_rng(3)
+    x = random_input(req, rng)
+    if dist == "spread":
+        x = x * np.exp2(rng.uniform(-40, 40, x.size))
+    elif dist == "spike":
+        x = x * 1e-6
+        x[1000] = 1500.0
+    else:
+        x.reshape(-1, 256)[17] *= 1e6
+    ref = oracle_run(req, x)
+    e_fx = rel_l2(gpu_run(req, x, prec="double"), ref)
+    e_nat = rel_l2(gpu_run(req, x, prec="double-f64"), ref)
+    assert e_fx <= 1.25 * e_nat + 1e-17, (e_fx, e_nat)
+
+
+@pytest.mark.parametrize("k", [-1000, -200, -1, 7, 300, 900])
+def test_fx_power_of_two_scaling_is_exact(cuda, pfft_lib, k):
+    """The grid follows the tile's exponent, so scaling the input by 2^k
+    scales every stored result by exactly 2^k (away from overflow and from
+    results below 2^-1022, which are stored as zero)."""
+    req = Req("c2c", (32, 64, 16))
+    x = random_input(req, np.random.default_rng(9))
+    base = gpu_run(req, x, prec="double")
+    got = gpu_run(req, np.ldexp(x, k), prec="double")
+    want = np.ldexp(base, k)
+    tiny = np.abs(want) < 2.0 ** -1000
+    assert np.array_equal(got[~tiny], want[~tiny])
+
+
+def test_fx_zeros_and_nonfinite(cuda, pfft_lib):
+    req = Req("c2c", (16, 16, 64))
+    x = np.zeros(req.counts()[0])
+    assert np.array_equal(gpu_run(req, x, prec="double"), np.zeros_like(x))
+    x = random_input(req, np.random.default_rng(1))
+    x[77] = np.inf
+    out = gpu_run(req, x, prec="double")
+    assert np.isnan(out).any() and not np.isinf(out).any()
+    x[77] = np.nan
+    assert np.isnan(gpu_run(req, x, prec="double")).any()
+
+
+def test_fx_large_transform_against_oracle(cuda, pfft_lib):
+    """256^3 complex128, forward: FX and native FP64 against the oracle."""
+    req = Req("c2c", (256, 256, 256))
+    x = random_input(req, np.random.default_rng(12))
+    ref = oracle_run(req, x)
+    e_fx = rel_l2(gpu_run(req, x, prec="double"), ref)
+    e_nat = rel_l2(gpu_run(req, x, prec="double-f64"), ref)
+    assert e_fx <= 1e-15 and e_fx <= 1.25 * e_nat, (e_fx, e_nat)

@@ -64,6 +64,12 @@ def run_gc(torch, kind, n, gcb, gca, prec="double", flags=0, howmany=1, reduce=F
     ("r", [6, 7, 8], [1, 1, 1], [1, 1, 1], pg.PFFT_GC_PADDED),
     ("c", [6, 7, 8], [1, 0, 2], [0, 1, 1], pg.PFFT_GC_R2C),
     ("c", [6, 7, 8], [1, 0, 2], [0, 1, 1], pg.PFFT_GC_TRANSPOSED),
+    # many chunks of the in-place move: no halo below (rows barely move),
+    # one-cell rows, long rows beyond the staging area (copy + gather path)
+    ("r", [64, 48, 40], [3, 0, 1], [0, 2, 5], 0),
+    ("c", [40, 64, 33], [0, 0, 0], [0, 0, 3], 0),
+    ("r", [50, 40, 1], [2, 3, 0], [1, 0, 0], 0),
+    ("c", [4, 3, 2100], [1, 1, 1], [1, 1, 1], 0),
 ])
 def test_exchange_bit_exact(cuda, pfft_lib, prec, kind, n, gcb, gca, flags):
     if flags & pg.PFFT_GC_TRANSPOSED:
@@ -80,10 +86,17 @@ def test_exchange_bit_exact(cuda, pfft_lib, prec, kind, n, gcb, gca, flags):
 
 @pytest.mark.parametrize("prec,tol", [("double", 1e-14), ("float", 1e-6)])
 def test_reduce(cuda, pfft_lib, prec, tol):
-    for n, gcb, gca in [([8, 8, 8], [0, 0, 0], [4, 0, 0]), ([5, 6, 7], [7, 1, 0], [0, 9, 2])]:
-        got, ref = run_gc(cuda, "c", n, gcb, gca, prec, reduce=True)
+    for kind, n, gcb, gca in [("c", [8, 8, 8], [0, 0, 0], [4, 0, 0]), ("c", [5, 6, 7], [7, 1, 0], [0, 9, 2]),
+                              ("r", [64, 48, 40], [3, 0, 1], [0, 2, 5]), ("c", [40, 64, 33], [0, 0, 0], [0, 0, 3]),
+                              ("r", [50, 40, 1], [2, 3, 0], [1, 0, 0]), ("c", [4, 3, 2100], [1, 1, 1], [1, 1, 1])]:
+        got, ref = run_gc(cuda, kind, n, gcb, gca, prec, reduce=True)
         err = np.linalg.norm(got - ref) / np.linalg.norm(ref)
-        assert err < tol
+        assert err < tol, (n, err)
+
+
+def test_reduce_256_width2(cuda, pfft_lib):
+    got, ref = run_gc(cuda, "r", [256, 256, 256], [2, 2, 2], [2, 2, 2], "double", reduce=True)
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-14
 
 
 def test_exchange_reduce_roundtrip_simple_check_ghost(cuda, pfft_lib):
