@@ -138,8 +138,9 @@ static bool fast_tables(const PassParams& p, int arith, bool pow2, const void** 
   cudaError_t e;
   const bool dct = p.mode == MODE_RE10 || p.mode == MODE_RE01;
   const int fsign = p.mode == MODE_RE10 ? -1 : (p.mode == MODE_RE01 ? 1 : p.sign);
-  if (arith == ARITH_F64) {  // 64-bit fixed point (FX), plain power-of-two c2c only
+  if (arith == ARITH_F64) {  // 64-bit fixed point (FX): power-of-two lines
     *tw = twiddle_table(p.N, fsign < 0 ? TW_FX_FWD_STG : TW_FX_BWD_STG, &e);
+    if (dct) *tw2 = twiddle_table(p.M, fsign < 0 ? TW_FX_FWD : TW_FX_BWD, &e);
   } else if (arith == ARITH_DF) {
     *tw = twiddle_table(p.N, pow2 ? (fsign < 0 ? TW_DFP_FWD_STG : TW_DFP_BWD_STG) : (fsign < 0 ? TW_DFP_FWD : TW_DFP_BWD),
                         &e);
@@ -163,10 +164,11 @@ bool fast_args(const PassParams& p, int arith, FastArgs* a, bool* row_in, bool* 
   if (!pow2 && (!mixed_supported(N) || !plain)) return false;
   if ((p.mode == MODE_RE10 || p.mode == MODE_RE01) && N > 512) return false;
   // double plans (native FP64 storage and arithmetic class): the radix-8
-  // kernel's 64-bit fixed-point arithmetic on plain power-of-two c2c lines
+  // kernel's 64-bit fixed-point arithmetic on power-of-two c2c, r2c, c2r,
+  // REDFT10 and REDFT01 lines with any window or adjoint weight
   // (PassParams::quant == 2); every other pass of such a plan runs the
   // general kernel in FP64
-  if (arith == ARITH_F64 && !(p.quant == 2 && pow2 && plain)) return false;
+  if (arith == ARITH_F64 && !(p.quant == 2 && pow2)) return false;
   if (arith != ARITH_F32 && arith != ARITH_DF && arith != ARITH_F64) return false;
   if (p.ashI.en || p.ashO.en) return false;
   if (p.nb > PG_MAX_BATCH) return false;
@@ -238,6 +240,8 @@ int launch_fast_pass(const PassParams& p, int arith, cudaStream_t stream) {
   a.staged = p.staged;
   // the FFT direction: the pass's, except for the DCTs (10 forward, 01 inverse)
   const int sign = a.mode == 3 ? -1 : (a.mode == 4 ? 1 : p.sign);
+  if (a.mode >= 3 && arith == ARITH_F64)
+    return sign < 0 ? launch_dct<FX, -1>(N, a, row_in, row_out, stream) : launch_dct<FX, 1>(N, a, row_in, row_out, stream);
   if (a.mode >= 3)
     return arith == ARITH_F32 ? (sign < 0 ? launch_dct<F32, -1>(N, a, row_in, row_out, stream)
                                           : launch_dct<F32, 1>(N, a, row_in, row_out, stream))
@@ -260,17 +264,20 @@ int launch_fast_pass(const PassParams& p, int arith, cudaStream_t stream) {
                       : (three ? launch_mixed_three<FDD, 1>(N, a, row_in, row_out, stream)
                                : launch_mixed_five<FDD, 1>(N, a, row_in, row_out, stream));
   }
-  if (!a.plain)  // r2c / c2r / windows / weights: the general-I/O instantiations
+  if (!a.plain) {  // r2c / c2r / windows / weights: the general-I/O instantiations
+    if (arith == ARITH_F64)
+      return sign < 0 ? launch_gio<FX, -1>(N, a, row_in, row_out, stream) : launch_gio<FX, 1>(N, a, row_in, row_out, stream);
     return arith == ARITH_F32 ? (sign < 0 ? launch_gio<F32, -1>(N, a, row_in, row_out, stream)
                                           : launch_gio<F32, 1>(N, a, row_in, row_out, stream))
                               : (sign < 0 ? launch_gio<FDD, -1>(N, a, row_in, row_out, stream)
                                           : launch_gio<FDD, 1>(N, a, row_in, row_out, stream));
+  }
   if (arith == ARITH_F32) {
     if (sign < 0)
       return big ? launch_large<F32, -1>(N, a, row_in, row_out, stream) : launch_small<F32, -1>(N, a, row_in, row_out, stream);
     return big ? launch_large<F32, 1>(N, a, row_in, row_out, stream) : launch_small<F32, 1>(N, a, row_in, row_out, stream);
   }
-  if (arith == ARITH_F64) {  // 64-bit fixed-point radix-8 stages (fast_args admitted plain c2c only)
+  if (arith == ARITH_F64) {  // 64-bit fixed-point radix-8 stages (plain c2c)
     if (sign < 0)
       return big ? launch_large<FX, -1>(N, a, row_in, row_out, stream) : launch_small<FX, -1>(N, a, row_in, row_out, stream);
     return big ? launch_large<FX, 1>(N, a, row_in, row_out, stream) : launch_small<FX, 1>(N, a, row_in, row_out, stream);

@@ -360,28 +360,34 @@ __device__ __forceinline__ void bf8x(typename P::C* v) {
 // m * 2^(e - 1075) (53-bit mantissa m) becomes X = (m << 5) >> (E - e), so
 // x = X * 2^(E - 1080) and |X| < 2^58: 58 significant bits against the
 // tile's largest component (a double holds 53 against its own magnitude).
-// Additions and subtractions are exact 64-bit integer operations.  Every
-// stage but the first multiplies by twiddles scaled by 1/8 (element 0 of a
-// butterfly, whose twiddle is 1, is shifted right by 3), which cancels the
-// radix-8 stage's growth: a butterfly's inputs have modulus below 2^58.5,
-// its partial sums and outputs below 2^61.5, the twiddle product's sum
-// a.re + a.im below 2^62.5 < 2^63, so nothing overflows.  Products are
-// 64 x 64 -> high 64 bits from 32-bit pieces (fx_mh: the low-by-low part and
-// the carries of the cross terms are dropped, error within 2 units of the
-// result), complex products in Gauss's three-multiplication form, the
-// sqrt(1/2) products of the butterflies as a - a (1 - sqrt(1/2)).  Every
-// rounding is a few units at 2^-58 of the tile's magnitude, below the
-// 2^-53 relative rounding of FP64 arithmetic.  Results are rounded to
-// nearest double when stored (x = Y * 2^(E - 1080 + 3 * twiddled stages)).
-// A tile holding an infinity or NaN stores NaN everywhere; results below
-// 2^-1022 are stored as zero.
+// Additions and subtractions are exact 64-bit integer operations.  Before
+// every stage but the first the tile is renormalised (block floating point
+// per stage): at the shared-memory exchange each warp ORs the high words of
+// its values' magnitudes, the tile's OR gives the bit length of its largest
+// component (within one bit), and every value is shifted left or right by
+// the same amount so that the largest stays below 2^60 (fx_normalise).  The
+// stage's twiddles are scaled by 1/4 (element 0 of a butterfly, whose
+// twiddle is 1, is shifted right by 2), so a butterfly's inputs have modulus
+// below 2^58.5, its partial sums and outputs below 2^61.5 and the twiddle
+// product's sum a.re + a.im below 2^61: nothing overflows whatever the
+// data, and data that does not grow (a spike spreading into a flat
+// spectrum) keeps its bits instead of paying for the worst-case growth.
+// Products are 64 x 64 -> high 64 bits from 32-bit pieces (mh: the
+// low-by-low part and the carries of the cross terms are dropped, error
+// within 2 units of the result), complex products in Gauss's
+// three-multiplication form, the sqrt(1/2) products of the butterflies as
+// a - a (1 - sqrt(1/2)).  Every rounding is a few units at 2^-58..2^-56 of
+// the tile's current magnitude, below the 2^-53 relative rounding of FP64
+// arithmetic.  Results are rounded to nearest double when stored
+// (x = Y * 2^(E - 1080 + the stages' shifts)).  A tile holding an infinity
+// or NaN stores NaN everywhere; results below 2^-1022 are stored as zero.
 struct FX {
   typedef longlong2 S;  // shared memory: (re, im)
   typedef double2 G;
   struct C {
     long long x, y;
   };
-  // twiddle w / 8 (stored as (hi, lo) with lo in [-2^31, 2^31), value hi * 2^32
+  // twiddle w / 4 (stored as (hi, lo) with lo in [-2^31, 2^31), value hi * 2^32
   // + lo, scaled by 2^64): r = Re w, d = Im w - Re w, s = Re w + Im w
   struct W {
     int2 r, d, s;
@@ -397,13 +403,15 @@ struct FX {
   static __device__ __forceinline__ C lds(const S& s) { return {s.x, s.y}; }
   static __device__ __forceinline__ S sts(C v) { return make_longlong2(v.x, v.y); }
   // floor(x * w / 2^64) up to a few units: x = xh 2^32 + xl, w = wh 2^32 + wl
-  // with signed low halves; the cross terms' high words and xh * wh
+  // with signed low halves; the cross terms' high words and xh * wh.  With
+  // |x| < 2^62.5 and |w| < 2^62.5 the cross terms' high words are below 2^30
+  // each, so their sum is a 32-bit add.
   static __device__ __forceinline__ long long mh(long long x, int2 w) {
     const unsigned xu = (unsigned)x;
     const int xl = (int)xu;
     const int xh = (int)(x >> 32) + (int)(xu >> 31);
-    const long long c = (long long)__mulhi(xh, w.y) + (long long)__mulhi(xl, w.x) + 1;
-    return (long long)xh * w.x + c;
+    const int c = __mulhi(xh, w.y) + __mulhi(xl, w.x) + 1;
+    return (long long)xh * w.x + (long long)c;
   }
   static __device__ __forceinline__ C mul(C a, const W& w) {
     const long long k1 = mh(a.x + a.y, w.r);
@@ -416,8 +424,8 @@ struct FX {
     const int2 k = make_int2(1257966796, 102865788);  // (1 - sqrt(1/2)) 2^64
     return {a.x - mh(a.x, k), a.y - mh(a.y, k)};
   }
-  // element 0 of a twiddled stage (twiddle 1, scaled by 1/8)
-  static __device__ __forceinline__ C tw0(C a) { return {a.x >> 3, a.y >> 3}; }
+  // element 0 of a twiddled stage (twiddle 1, scaled by 1/4, rounded to nearest)
+  static __device__ __forceinline__ C tw0(C a) { return {(a.x + 2) >> 2, (a.y + 2) >> 2}; }
   static __device__ __forceinline__ W ldw(const void* base, int idx, int cnt) {
     const int2* t = (const int2*)base;
     return {__ldg(t + idx), __ldg(t + cnt + idx), __ldg(t + 2 * cnt + idx)};
@@ -487,10 +495,55 @@ __device__ __forceinline__ int fx_enter(FX::C (&v)[8], int conj_in) {
     v[r].y = fx_from_bits(v[r].y, E);
     if (conj_in) v[r].y = -v[r].y;
   }
-  constexpr int NS8 = N >= 4096 ? 4 : (N >= 512 ? 3 : (N >= 64 ? 2 : 1));
-  constexpr int P8 = NS8 == 4 ? 4096 : (NS8 == 3 ? 512 : (NS8 == 2 ? 64 : 8));
-  constexpr int TWST = NS8 - 1 + (N / P8 > 1 ? 1 : 0);  // stages with (scaled) twiddles
-  return Eraw == 0x7FF ? INT_MIN : E - 1080 + 3 * TWST;
+  return Eraw == 0x7FF ? INT_MIN : E - 1080;
+}
+
+// Block normalisation of a stage (see FX): fx_ormag before the exchange's
+// barrier (each warp's OR of |high words| into slot[warp]), fx_normal_shift
+// after it (the tile's shift: the largest component below 2^60), fx_shift
+// on every value.
+__device__ __forceinline__ unsigned fx_ormag(const FX::C (&v)[8]) {
+  unsigned acc = 0;
+#pragma unroll
+  for (int r = 0; r < 8; r++) {
+    const int hx = (int)(v[r].x >> 32), hy = (int)(v[r].y >> 32);
+    acc |= (unsigned)(hx ^ (hx >> 31)) | (unsigned)(hy ^ (hy >> 31));
+  }
+  return acc;
+}
+__device__ __forceinline__ void fx_ormag_publish(unsigned m, unsigned* slot) {
+  m = __reduce_or_sync(0xffffffffu, m);
+  if ((threadIdx.x & 31) == 0) slot[threadIdx.x >> 5] = m;
+}
+// right shift (> 0) or left shift (< 0) bringing the bit length of the
+// tile's largest component to at most 60 (the OR of the high words gives it
+// within one bit: an exact negative power of two reads one bit short)
+__device__ __forceinline__ int fx_normal_shift(const unsigned* slot) {
+  const int lane = threadIdx.x & 31;
+  unsigned m = lane < (int)(blockDim.x >> 5) ? slot[lane] : 0u;
+  m = __reduce_or_sync(0xffffffffu, m);
+  const int bl = 32 + (m ? 32 - __clz((int)m) : 0);
+  return bl - 59;
+}
+// x * 2^-s for -31 < s < 32, rounded to nearest (the same s in every thread:
+// no divergence)
+__device__ __forceinline__ long long fx_shift(long long x, int s) {
+  if (s > 0) x += 1ll << (s - 1);
+  unsigned lo = (unsigned)x;
+  int hi = (int)(x >> 32);
+  if (s >= 0) {
+    lo = __funnelshift_r(lo, (unsigned)hi, s);
+    hi = hi >> s;
+  } else {
+    const int t = -s;
+    hi = (int)__funnelshift_l(lo, (unsigned)hi, t);
+    lo = lo << t;
+  }
+  return (long long)(((unsigned long long)(unsigned)hi << 32) | lo);
+}
+__device__ __forceinline__ unsigned* fx_slots() {
+  __shared__ unsigned slots[2][32];  // per-warp ORs of two consecutive stages
+  return &slots[0][0];
 }
 
 // Shared-memory layout of a tile: L lines at stride lsp_of, element p of a
@@ -643,15 +696,29 @@ template <>
 __device__ __forceinline__ FDD::C rload<FDD, true>(const void* src, long long i) {
   return FDD::from_df(df_from_double(__ldcg((const double*)src + i)), df{0.f, 0.f});
 }
-template <class P>
-__device__ __forceinline__ void rstore(void* dst, long long i, typename P::C v);
+// FX: the double's raw bits (converted by fx_enter), zero imaginary part
 template <>
-__device__ __forceinline__ void rstore<F32>(void* dst, long long i, F32::C v) {
+__device__ __forceinline__ FX::C rload<FX, false>(const void* src, long long i) {
+  return {__double_as_longlong(((const double*)src)[i]), 0ll};
+}
+template <>
+__device__ __forceinline__ FX::C rload<FX, true>(const void* src, long long i) {
+  return {__double_as_longlong(__ldcg((const double*)src + i)), 0ll};
+}
+// eo: FX's result exponent (fx_enter), unused by the other policies
+template <class P>
+__device__ __forceinline__ void rstore(void* dst, long long i, typename P::C v, int eo);
+template <>
+__device__ __forceinline__ void rstore<F32>(void* dst, long long i, F32::C v, int) {
   ((float*)dst)[i] = v.x;
 }
 template <>
-__device__ __forceinline__ void rstore<FDD>(void* dst, long long i, FDD::C v) {
+__device__ __forceinline__ void rstore<FDD>(void* dst, long long i, FDD::C v, int) {
   ((double*)dst)[i] = df_to_double_sel(FDD::re_df(v));
+}
+template <>
+__device__ __forceinline__ void rstore<FX>(void* dst, long long i, FX::C v, int eo) {
+  ((double*)dst)[i] = fx_to_double(v.x, eo);
 }
 template <class P>
 __device__ __forceinline__ typename P::C czero();
@@ -659,6 +726,15 @@ template <>
 __device__ __forceinline__ F32::C czero<F32>() { return make_float2(0.f, 0.f); }
 template <>
 __device__ __forceinline__ FDD::C czero<FDD>() { return {make_float2(0.f, 0.f), make_float2(0.f, 0.f)}; }
+template <>
+__device__ __forceinline__ FX::C czero<FX>() { return {0ll, 0ll}; }
+// FX before fx_enter: conjugation and halving of the raw doubles
+__device__ __forceinline__ FX::C fx_conj_raw(FX::C v) {
+  return {v.x, (long long)((unsigned long long)v.y ^ 0x8000000000000000ull)};
+}
+__device__ __forceinline__ FX::C fx_half_raw(FX::C v) {
+  return {__double_as_longlong(__longlong_as_double(v.x) * 0.5), __double_as_longlong(__longlong_as_double(v.y) * 0.5)};
+}
 
 // real input x_j of a real-to-real line (zero outside the embedded range)
 template <class P, bool CG>
@@ -678,8 +754,13 @@ __device__ __forceinline__ typename P::C load_elem(const FastArgs& a, long long 
     if (a.mode == 3) return rx<P, CG>(a, off, 2 * e < N ? 2 * e : 2 * (N - 1 - e) + 1);
     C xk = rx<P, CG>(a, off, e);
     C xm = e == 0 ? czero<P>() : rx<P, CG>(a, off, N - e);
-    C z = P::sub(xk, P::swap_neg_re(xm));  // x_k - i x_(N-k)
-    return P::mul(z, P::template twd<1>(P::ldw(a.tw2, e, 4 * N)));
+    if constexpr (is_fx<P>()) {
+      // raw x_k - i x_(N-k); the rotation by W_4N^-k follows fx_enter (fast_body)
+      return {xk.x, (long long)((unsigned long long)xm.x ^ 0x8000000000000000ull)};
+    } else {
+      C z = P::sub(xk, P::swap_neg_re(xm));  // x_k - i x_(N-k)
+      return P::mul(z, P::template twd<1>(P::ldw(a.tw2, e, 4 * N)));
+    }
   }
   bool mirror = false;
   int q, k = e;
@@ -691,18 +772,27 @@ __device__ __forceinline__ typename P::C load_elem(const FastArgs& a, long long 
   if (q < 0 || q >= a.Ni) return czero<P>();
   C v = a.mode == 1 ? rload<P, CG>(a.src, off + (long long)q * a.sIa)
                     : gload<P, CG>((const typename P::G*)a.src + off + (long long)q * a.sIa, a.in_df);
-  if (a.conj_in) v = P::conj(v);
-  if (a.wmode == 1 && k != 0 && 2 * k != N) v = P::scal(v, PG_KC(P, 0.5));
-  return mirror ? P::conj(v) : v;
+  if constexpr (is_fx<P>()) {  // raw doubles until fx_enter
+    if (a.conj_in) v = fx_conj_raw(v);
+    if (a.wmode == 1 && k != 0 && 2 * k != N) v = fx_half_raw(v);
+    return mirror ? fx_conj_raw(v) : v;
+  } else {
+    if (a.conj_in) v = P::conj(v);
+    if (a.wmode == 1 && k != 0 && 2 * k != N) v = P::scal(v, PG_KC(P, 0.5));
+    return mirror ? P::conj(v) : v;
+  }
 }
 
 // store logical output position e of a line (kept when Zo <= e < Zo + No)
+// (eo: FX's result exponent)
 template <class P, bool DCT = false>
-__device__ __forceinline__ void store_elem(const FastArgs& a, long long off, int e, typename P::C v, int N) {
+__device__ __forceinline__ void store_elem(const FastArgs& a, long long off, int e, typename P::C v, int N,
+                                           int eo = 0) {
   if constexpr (DCT) {
     if (a.mode == 3) {  // y_e = 2 Re(W_4N^e V_e)
       v = P::mul(v, P::template twd<-1>(P::ldw(a.tw2, e, 4 * N)));
       v = P::add(v, v);
+      if constexpr (is_fx<P>()) eo = eo == INT_MIN ? eo : eo + 2;  // FX twiddles carry 1/4
     } else {
       e = 2 * e < N ? 2 * e : 2 * (N - 1 - e) + 1;
     }
@@ -712,9 +802,9 @@ __device__ __forceinline__ void store_elem(const FastArgs& a, long long off, int
   if (a.wmode == 2 && e != 0 && 2 * e != N) v = P::add(v, v);
   if (a.conj_out) v = P::conj(v);
   if (a.mode >= 2)
-    rstore<P>(a.dst, off + (long long)k * a.sOa, v);
+    rstore<P>(a.dst, off + (long long)k * a.sOa, v, eo);
   else
-    gstore<P>((typename P::G*)a.dst + off + (long long)k * a.sOa, v, a.out_df);
+    gstore<P>((typename P::G*)a.dst + off + (long long)k * a.sOa, v, is_fx<P>() ? eo : a.out_df);
 }
 
 // ROW_IN: the axis is contiguous on the input side (thread t walks the line);
@@ -799,13 +889,24 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
   constexpr int TWN = fast_tw_n(N);
   S* line = buf + l * LSP;
   int sdf = a.out_df;  // FX: the results' exponent instead
-  if constexpr (is_fx<P>()) sdf = fx_enter<N>(v, a.conj_in);
+  int fx_e = 0, fx_sh = 0;  // FX: the tile's grid exponent and the stages' shifts
+  if constexpr (is_fx<P>()) {
+    fx_e = fx_enter<N>(v, IO == 0 ? a.conj_in : 0);  // IO 1: conjugated in load_elem
+    if constexpr (IO == 2) {
+      if (a.mode == 4) {  // REDFT01: (x_k - i x_(N-k)) W_4N^-k, twiddles carrying 1/4
+#pragma unroll
+        for (int r = 0; r < 8; r++) v[r] = P::mul(v[r], P::template twd<1>(P::ldw(a.tw2, t + r * TPL, 4 * N)));
+        fx_sh += 2;
+      }
+    }
+  }
   bf8x<P, SIGN>(v);  // stage 0 (Ns = 1, no twiddles)
   int Ns = 1;
   // radix-8 stages 1 .. NS8-1 through shared memory
 #pragma unroll
   for (int s = 1; s < NS8; s++) {
     if (s > 1) __syncthreads();  // previous stage's loads are done
+    if constexpr (is_fx<P>()) fx_ormag_publish(fx_ormag(v), fx_slots() + 32 * (s & 1));
     {
       const int k = t % Ns;
       const int base = (t - k) * 8 + k;
@@ -816,12 +917,19 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
     Ns *= 8;
 #pragma unroll
     for (int r = 0; r < 8; r++) v[r] = P::lds(line[pad<P>(t + r * TPL)]);
+    if constexpr (is_fx<P>()) {
+      const int sh = fx_normal_shift(fx_slots() + 32 * (s & 1));
+#pragma unroll
+      for (int r = 0; r < 8; r++) v[r] = {fx_shift(v[r].x, sh), fx_shift(v[r].y, sh)};
+      fx_sh += sh + 2;
+    }
     const int k = t % Ns;
     v[0] = P::tw0(v[0]);
 #pragma unroll
     for (int r = 1; r < 8; r++) v[r] = P::mul(v[r], P::template twd<SIGN>(P::ldw(tw, Ns - 8 + (r - 1) * Ns + k, TWN)));
     bf8x<P, SIGN>(v);
   }
+  if constexpr (is_fx<P>()) sdf = fx_e == INT_MIN ? INT_MIN : fx_e + fx_sh;
   if (Q == 1) {
     // v holds the last stage (Ns = N/8, k = t): outputs y[t + r*TPL]
     if (ROW_IN == ROW_OUT) {
@@ -833,7 +941,7 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
           for (int r = 0; r < 8; r++) gstore<P>(dst + r * st, a.conj_out ? P::conj(v[r]) : v[r], sdf);
         } else {
 #pragma unroll
-          for (int r = 0; r < 8; r++) store_elem<P, IO == 2>(a, offO[l], t + r * TPL, v[r], N);
+          for (int r = 0; r < 8; r++) store_elem<P, IO == 2>(a, offO[l], t + r * TPL, v[r], N, sdf);
         }
       }
       return;
@@ -844,6 +952,7 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
   } else {
     // radix-Q stage (Q = 2 or 4) with Ns = N/Q: butterflies j = t + b*TPL, k = j
     if (NS8 > 1) __syncthreads();
+    if constexpr (is_fx<P>()) fx_ormag_publish(fx_ormag(v), fx_slots() + 32 * (NS8 & 1));
     {
       const int k = t % Ns;
       const int base = (t - k) * 8 + k;
@@ -853,6 +962,12 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
     __syncthreads();
     constexpr int NB = 8 / Q;
     constexpr int NQ = N / Q;
+    int qsh = 0;
+    if constexpr (is_fx<P>()) {
+      qsh = fx_normal_shift(fx_slots() + 32 * (NS8 & 1));
+      fx_sh += qsh + 2;
+      sdf = fx_e == INT_MIN ? INT_MIN : fx_e + fx_sh;
+    }
     C w[8];
 #pragma unroll
     for (int b = 0; b < NB; b++) {
@@ -860,6 +975,7 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
 #pragma unroll
       for (int r = 0; r < Q; r++) {
         C x = P::lds(line[pad<P>(j + r * NQ)]);
+        if constexpr (is_fx<P>()) x = {fx_shift(x.x, qsh), fx_shift(x.y, qsh)};
         x = r > 0 ? P::mul(x, P::template twd<SIGN>(P::ldw(tw, NQ - 8 + (r - 1) * NQ + j, TWN))) : P::tw0(x);
         w[b * Q + r] = x;
       }
@@ -886,7 +1002,7 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
 #pragma unroll
           for (int b = 0; b < NB; b++)
 #pragma unroll
-            for (int r = 0; r < Q; r++) store_elem<P, IO == 2>(a, offO[l], t + b * TPL + r * NQ, w[b * Q + r], N);
+            for (int r = 0; r < Q; r++) store_elem<P, IO == 2>(a, offO[l], t + b * TPL + r * NQ, w[b * Q + r], N, sdf);
         }
       }
       return;
@@ -913,7 +1029,7 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
           if (a.conj_out) o = P::conj(o);
           gstore<P>(d2 + (long long)k * a.sOa, o, sdf);
         } else {
-          store_elem<P, IO == 2>(a, offO[l2], k, o, N);
+          store_elem<P, IO == 2>(a, offO[l2], k, o, N, sdf);
         }
       }
     }

@@ -1,0 +1,31 @@
+// Instantiation unit of the radix-8 pass kernel for r2c / c2r / windowed /
+// weighted passes (load_elem, store_elem in fft_fast.cuh), 64-bit fixed point (FX), backward,
+// 16..4096-point lines, default tile heights.
+#include "fft_fast.cuh"
+
+namespace pg {
+namespace fast {
+
+template <class P, int SIGN>
+int launch_gio(int N, const FastArgs& a, bool row_in, bool row_out, cudaStream_t s) {
+  const bool col = !(row_in && row_out);
+  switch (N) {
+    case 16: return launch4<P, SIGN, 16, 128, 1>(a, row_in, row_out, s);
+    case 32: return launch4<P, SIGN, 32, 64, 1>(a, row_in, row_out, s);
+    case 64: return launch4<P, SIGN, 64, 32, 1>(a, row_in, row_out, s);
+    case 128: return launch4<P, SIGN, 128, 16, 1>(a, row_in, row_out, s);
+    case 256: return launch4<P, SIGN, 256, 8, 1>(a, row_in, row_out, s);
+    case 512: return col ? launch4<P, SIGN, 512, 8, 1>(a, row_in, row_out, s)
+                         : launch4<P, SIGN, 512, 4, 1>(a, row_in, row_out, s);
+    case 1024: return col ? launch4<P, SIGN, 1024, 4, 1>(a, row_in, row_out, s)
+                          : launch4<P, SIGN, 1024, 2, 1>(a, row_in, row_out, s);
+    case 2048: return launch4<P, SIGN, 2048, 2, 1>(a, row_in, row_out, s);
+    case 4096: return launch4<P, SIGN, 4096, 1, 1>(a, row_in, row_out, s);
+  }
+  return -1;
+}
+
+template int launch_gio<FX, 1>(int, const FastArgs&, bool, bool, cudaStream_t);
+
+}  // namespace fast
+}  // namespace pg

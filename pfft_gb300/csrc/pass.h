@@ -25,7 +25,7 @@ enum ArithId { ARITH_F32 = 0, ARITH_F64 = 1, ARITH_DF = 2 };
 // low parts (FDD::W).
 //   TW_FX_FWD_STG / _BWD_STG: the radix-8 kernel's stage-major tables for the
 //     64-bit fixed-point arithmetic (FX::W): three arrays of int2, Re w,
-//     Im w - Re w and Re w + Im w, each scaled by 2^61 (w / 8 in units of
+//     Im w - Re w and Re w + Im w, each scaled by 2^62 (w / 4 in units of
 //     2^-64) and split as hi * 2^32 + lo with lo in [-2^31, 2^31).
 enum TwiddleKind {
   TW_DFP_FWD = 16,
@@ -34,7 +34,9 @@ enum TwiddleKind {
   TW_DFP_FWD_STG = 19,
   TW_DFP_BWD_STG = 20,
   TW_FX_FWD_STG = 21,
-  TW_FX_BWD_STG = 22
+  TW_FX_BWD_STG = 22,
+  TW_FX_FWD = 23,  // the same format in natural order (the DCTs' length-4N rotations)
+  TW_FX_BWD = 24
 };
 // entries of a stage-major table for a power-of-two N >= 16
 inline int fast_tw_count(int N) {

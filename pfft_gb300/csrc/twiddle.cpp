@@ -57,9 +57,9 @@ void packed_entry(long double c, long double s, float* h, float* l) {
   h[0] = rh; h[1] = rh; h[2] = -ih; h[3] = ih;
   l[0] = rl; l[1] = rl; l[2] = -il; l[3] = il;
 }
-// v * 2^61 rounded to an integer, split as hi * 2^32 + lo, lo in [-2^31, 2^31)
+// v * 2^62 rounded to an integer, split as hi * 2^32 + lo, lo in [-2^31, 2^31)
 void fx_split(long double v, int* hl) {
-  const long long x = llroundl(ldexpl(v, 61));
+  const long long x = llroundl(ldexpl(v, 62));
   const long long hi = (x + (1ll << 31)) >> 32;
   hl[0] = (int)hi;
   hl[1] = (int)(x - hi * (1ll << 32));
@@ -71,10 +71,11 @@ const void* twiddle_table(int M, int arith, cudaError_t* err) {
   auto key = std::make_pair(M, arith);
   auto it = g_tables.find(key);
   if (it != g_tables.end()) return it->second;
-  const bool fx = arith == TW_FX_FWD_STG || arith == TW_FX_BWD_STG;
-  const bool staged = arith == TW_F32_STG || arith == TW_DFP_FWD_STG || arith == TW_DFP_BWD_STG || fx;
+  const bool fx = arith == TW_FX_FWD_STG || arith == TW_FX_BWD_STG || arith == TW_FX_FWD || arith == TW_FX_BWD;
+  const bool staged = arith == TW_F32_STG || arith == TW_DFP_FWD_STG || arith == TW_DFP_BWD_STG ||
+                      arith == TW_FX_FWD_STG || arith == TW_FX_BWD_STG;
   const bool packed = arith == TW_DFP_FWD || arith == TW_DFP_BWD || arith == TW_DFP_FWD_STG || arith == TW_DFP_BWD_STG;
-  const bool bwd = arith == TW_DFP_BWD || arith == TW_DFP_BWD_STG || arith == TW_FX_BWD_STG;
+  const bool bwd = arith == TW_DFP_BWD || arith == TW_DFP_BWD_STG || arith == TW_FX_BWD_STG || arith == TW_FX_BWD;
   if (staged && (M < 16 || (M & (M - 1)))) {
     if (err) *err = cudaErrorInvalidValue;
     return nullptr;

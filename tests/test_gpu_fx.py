@@ -37,12 +37,41 @@ def test_fx_no_less_accurate_than_native_fp64(cuda, pfft_lib, n, flags, sign):
     assert e_fx <= 1.25 * e_nat + 1e-17, (e_fx, e_nat)
 
 
-@pytest.mark.parametrize("dist", ["spread", "spike", "one_line"])
-def test_fx_dynamic_range(cuda, pfft_lib, dist):
-    """Values spread over 2^+-40, a single large value among small ones, and
-    one line a million times larger than the others: FX's error, relative to
-    the result's norm, stays within native FP64's."""
-    req = Req("c2c", (64, 32, 128))
+def _exact_dft3(x, n, sign=-1):
+    """3-D DFT in extended precision (numpy longdouble: 64- or 113-bit
+    mantissa), one axis at a time by explicit DFT matrices: a reference more
+    accurate than either arithmetic under test (the FP64 oracle shares native
+    FP64's rounding pattern on sparse inputs, e.g. it reproduces a spike's
+    transform bit for bit)."""
+    ld = np.longdouble
+    pi = ld("3.14159265358979323846264338327950288")
+    a = (x[0::2].astype(ld) + x[1::2].astype(ld) * np.clongdouble(1j)).reshape(n)
+    for ax, m in enumerate(n):
+        k = np.arange(m)
+        # the angle from the integer numerator jk mod m keeps the table exact to longdouble
+        ph = np.mod(np.outer(k, k), m).astype(ld) * (2 * pi / ld(m))
+        W = np.cos(ph) + sign * np.clongdouble(1j) * np.sin(ph)
+        a = np.moveaxis(np.tensordot(W, np.moveaxis(a, ax, 0), axes=(1, 0)), 0, ax)
+    out = np.empty(2 * a.size, dtype=ld)
+    out[0::2] = a.real.ravel()
+    out[1::2] = a.imag.ravel()
+    return out
+
+
+def _rel(got, exact):
+    e = np.asarray(exact, dtype=np.longdouble)
+    return float(np.linalg.norm((np.asarray(got, dtype=np.longdouble) - e).astype(np.float64)) /
+                 np.linalg.norm(e.astype(np.float64)))
+
+
+@pytest.mark.parametrize("dist", ["uniform", "spread", "spike", "spike_alone", "one_line"])
+def test_fx_dynamic_range_against_extended_precision(cuda, pfft_lib, dist):
+    """Uniform values, values spread over 2^+-40, a single large value among
+    small ones (and alone), one line a million times larger than the rest:
+    FX's error against an extended-precision DFT stays within 1.25x native
+    FP64's error, or within one double rounding (2^-53) of the result."""
+    n = (8, 16, 32)
+    req = Req("c2c", n)
     rng = np.random.default_rng(3)
     x = random_input(req, rng)
     if dist == "spread":
@@ -50,12 +79,15 @@ def test_fx_dynamic_range(cuda, pfft_lib, dist):
     elif dist == "spike":
         x = x * 1e-6
         x[1000] = 1500.0
-    else:
-        x.reshape(-1, 256)[17] *= 1e6
-    ref = oracle_run(req, x)
-    e_fx = rel_l2(gpu_run(req, x, prec="double"), ref)
-    e_nat = rel_l2(gpu_run(req, x, prec="double-f64"), ref)
-    assert e_fx <= 1.25 * e_nat + 1e-17, (e_fx, e_nat)
+    elif dist == "spike_alone":
+        x = np.zeros_like(x)
+        x[1000] = 1500.0
+    elif dist == "one_line":
+        x.reshape(-1, 64)[17] *= 1e6
+    exact = _exact_dft3(x, n)
+    e_fx = _rel(gpu_run(req, x, prec="double"), exact)
+    e_nat = _rel(gpu_run(req, x, prec="double-f64"), exact)
+    assert e_fx <= max(1.25 * e_nat, 2.0 ** -53), (e_fx, e_nat)
 
 
 @pytest.mark.parametrize("k", [-1000, -200, -1, 7, 300, 900])
