@@ -63,7 +63,13 @@ int pfftf_gb300_plan_info(const pfftf_plan plan, int *npasses, double *bytes, si
  * kernel, -1 = no such pass. */
 int pfft_gb300_pass_kernel(const pfft_plan plan, int i);
 int pfftf_gb300_pass_kernel(const pfftf_plan plan, int i);
-/* Arithmetic a plan runs in: 0 FP32 (float API), 1 native FP64, 2 float-float. */
+/* Fixed-point mantissas kept across pass i's boundaries (double plans, mode
+ * 2): bit 0 = its input holds the previous pass's mantissas, bit 1 = its
+ * output keeps them for the next pass; -1 = no such pass. */
+int pfft_gb300_pass_fx_link(const pfft_plan plan, int i);
+int pfftf_gb300_pass_fx_link(const pfftf_plan plan, int i);
+/* Arithmetic a plan runs in: 0 FP32 (float API), 1 FP64 class (modes 1 and 2
+ * of pfft_gb300_set_double_arith), 2 float-float. */
 int pfft_gb300_plan_arith(const pfft_plan plan);
 int pfftf_gb300_plan_arith(const pfftf_plan plan);
 int pfft_gb300_pass_info(const pfft_plan plan, int i, int *axis, int *M, int *L, int *threads, int *smem,
@@ -113,22 +119,30 @@ int pfft_gb300_selftest_df_fast(const float *pairs, long long n, unsigned long l
 
 /* Arithmetic of the double API, for plans created afterwards:
  *   0  float-float on the FP32 pipes with TwoSum additions (48-49
- *      significant bits; relative L2 error of a transform about 1e-14)
- *   1  native FP64 (full double rounding; FP64 issues at about 1/64 of the
- *      FP32 rate on GB300)
- *   2  by size (default): native FP64 for transforms of at most 2^18 points
- *      (howmany included), mode 3 above.
+ *      significant bits; relative L2 error of a transform about 1e-14);
+ *      opt-in: narrower than FFTW double
+ *   1  native FP64 on every pass (general kernel; FP64 issues at about 1/70
+ *      of the FP32 rate on GB300)
+ *   2  default: FP64-class.  Power-of-two c2c, r2c, c2r, REDFT10 and REDFT01
+ *      passes run the radix-8 kernel in 64-bit block fixed point (int64
+ *      mantissas on a per-tile grid renormalised at every stage, exact
+ *      additions, 64-bit twiddles; measured as accurate as native FP64),
+ *      every other pass native FP64.
  *   3  float-float whose c2c passes on the radix-8 and mixed-radix kernels
  *      (2^a, 3 * 2^a, 5 * 2^a points) round the high words of each butterfly
  *      to a common grid, so that the butterfly's additions are exact without
- *      TwoSum: fewer FP32
- *      operations, relative L2 error about 2e-13 per pass (bounded by a
- *      small multiple of 2^-45 per radix-8 stage, relative to the data's L2
- *      norm); other passes as in mode 0.
+ *      TwoSum: fewer FP32 operations, relative L2 error about 2e-13 per
+ *      pass; other passes as in mode 0; opt-in: narrower than FFTW double.
  * The environment variable PFFT_GB300_F64_ARITH=df|native|auto|dfq sets the
  * initial mode.  Returns 0, or -1 for an unknown mode. */
 int pfft_gb300_set_double_arith(int mode);
 int pfft_gb300_get_double_arith(void);
+
+/* Mode 2 keeps the int64 mantissas (and one exponent per line) between two
+ * consecutive radix-8 passes instead of rounding them to double in between
+ * (on by default; the environment variable PFFT_GB300_FX_LINK=0 sets it off).
+ * Applies to plans created afterwards.  Returns the previous setting. */
+int pfft_gb300_set_fx_link(int on);
 
 /* Autotuning and wisdom.  Plans created with PFFT_PATIENT, PFFT_EXHAUSTIVE
  * or PFFT_TUNE time the candidate configurations of every pass (radix-8

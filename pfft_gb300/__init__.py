@@ -182,6 +182,8 @@ def _declare(L):
     L.pfft_gb300_last_error_string.restype = ctypes.c_char_p
     L.pfft_gb300_set_double_arith.argtypes = [ctypes.c_int]
     L.pfft_gb300_set_double_arith.restype = ctypes.c_int
+    L.pfft_gb300_set_fx_link.argtypes = [ctypes.c_int]
+    L.pfft_gb300_set_fx_link.restype = ctypes.c_int
     for nm in ("pfft_gb300_plan_arith", "pfftf_gb300_plan_arith"):
         getattr(L, nm).argtypes = [c_void_p]
         getattr(L, nm).restype = ctypes.c_int
@@ -193,6 +195,9 @@ def _declare(L):
     L.pfft_gb300_import_wisdom_from_filename.argtypes = [ctypes.c_char_p]
     L.pfft_gb300_import_wisdom_from_filename.restype = ctypes.c_int
     L.pfft_gb300_wisdom_entries.restype = ctypes.c_int
+    for nm in ("pfft_gb300_pass_fx_link", "pfftf_gb300_pass_fx_link"):
+        getattr(L, nm).argtypes = [c_void_p, ctypes.c_int]
+        getattr(L, nm).restype = ctypes.c_int
     for nm in ("pfft_gb300_pass_kernel", "pfftf_gb300_pass_kernel"):
         getattr(L, nm).argtypes = [c_void_p, ctypes.c_int]
         getattr(L, nm).restype = ctypes.c_int

@@ -376,6 +376,11 @@ void do_execute(Plan* pl, void* in, void* out) {
     if (!plan || i < 0 || i >= (int)plan->p->fwd.passes.size()) return -1;                                \
     return fast_pass_eligible(plan->p->fwd.passes[i].p, plan->p->arith) ? 1 : 0;                         \
   }                                                                                                       \
+  int PX##gb300_pass_fx_link(const PX##plan plan, int i) {                                              \
+    if (!plan || i < 0 || i >= (int)plan->p->fwd.passes.size()) return -1;                                \
+    const PassParams& q = plan->p->fwd.passes[i].p;                                                       \
+    return (q.fx_in ? 1 : 0) | (q.fx_out ? 2 : 0);                                                        \
+  }                                                                                                       \
   int PX##gb300_plan_arith(const PX##plan plan) {                                                        \
     if (!plan) return -1;                                                                                 \
     return plan->p->arith;                                                                                \
@@ -435,4 +440,9 @@ int pfft_gb300_set_double_arith(int mode) {
   return 0;
 }
 int pfft_gb300_get_double_arith(void) { return double_arith(); }
+int pfft_gb300_set_fx_link(int on) {
+  const int old = fx_link();
+  set_fx_link(on);
+  return old;
+}
 }

@@ -126,12 +126,31 @@ Batch* make_batch(Plan* const* plans, int n) {
     maxp = std::max(maxp, npass[i]);
     bool pr8 = true;  // every pass on the radix-8 tile
     int psmem = 0;
+    // radix-8 / mixed-radix tile when the pass qualifies (plain c2c lines
+    // of up to 512 (2^a) or 768 (3 * 2^a, 5 * 2^a) points with the same
+    // orientation on both sides), else a general tile
+    auto fast_tile_ok = [&](const PassParams& p, fast::FastArgs* fa, bool* ri, bool* ro) {
+      const bool pow2 = !(p.N & (p.N - 1));
+      return kernel_path() == 1 && p.kpath == 0 && p.N <= (pow2 ? 512 : 768) &&
+             fast::fast_args(p, pl->arith, fa, ri, ro) && *ri == *ro && fa->plain;
+    };
+    // FX mantissas kept between passes need the radix-8 tile on both sides;
+    // a plan with a linked pass that runs a general tile here gets double
+    // intermediates in the batch (results within rounding of its own
+    // executes instead of bit for bit)
+    bool unlink = false;
+    for (const Pass& ps : pl->fwd.passes) {
+      fast::FastArgs fa;
+      bool ri, ro;
+      if ((ps.p.fx_in || ps.p.fx_out) && !fast_tile_ok(ps.p, &fa, &ri, &ro)) unlink = true;
+    }
     for (const Pass& ps : pl->fwd.passes) {
       BatchPass bp;
       memset(&bp, 0, sizeof(bp));
       bp.p = ps.p;
       bp.p.src = bufs[ps.src];
       bp.p.dst = bufs[ps.dst];
+      if (unlink) bp.p.fx_in = bp.p.fx_out = 0;
       cudaError_t e;
       bp.arith = pl->arith;
       bp.p.tw = twiddle_table(ps.p.M, pl->arith, &e);
@@ -141,16 +160,12 @@ Batch* make_batch(Plan* const* plans, int n) {
         return nullptr;
       }
       bp.done = (int)hp.size();
-      // radix-8 / mixed-radix tile when the pass qualifies (plain c2c lines
-      // of up to 512 (2^a) or 768 (3 * 2^a, 5 * 2^a) points with the same
-      // orientation on both sides), else a general tile
       bool ri = false, ro = false;
       long long tiles;
       const bool pow2 = !(ps.p.N & (ps.p.N - 1));
       // (a pass the autotuner or wisdom put on the general kernel keeps it)
       // (r2c / c2r / windowed / DCT passes keep the general tile in a batch)
-      if (kernel_path() == 1 && ps.p.kpath == 0 && ps.p.N <= (pow2 ? 512 : 768) &&
-          fast::fast_args(bp.p, pl->arith, &bp.fa, &ri, &ro) && ri == ro && bp.fa.plain) {
+      if (fast_tile_ok(bp.p, &bp.fa, &ri, &ro)) {
         bp.fastN = ps.p.N;
         bp.frow = ri ? 1 : 0;
         bp.mixed = pow2 ? 0 : 1;
@@ -159,7 +174,7 @@ Batch* make_batch(Plan* const* plans, int n) {
                            : (pl->arith == ARITH_F32 ? fast::mixed_L<fast::F32>(bp.fastN) : fast::mixed_L<fast::FDD>(bp.fastN));
         tiles = (ps.p.nlines + L - 1) / L;
         const int lsp = fsz == 8 ? bp.fastN + 16 : bp.fastN + bp.fastN / 8 + 4;  // as fast_smem_bytes
-        psmem = std::max(psmem, (int)(16 * L + (size_t)L * lsp * fsz));
+        psmem = std::max(psmem, (int)((fsz == 8 ? 16 * L : (24 * L + 15) / 16 * 16) + (size_t)L * lsp * fsz));  // header: fast_hdr
         if (bp.mixed) pr8 = false;
         b->fast_passes++;
       } else {

@@ -173,6 +173,9 @@ struct Plan {
   cudaEvent_t pipe_ev[2][PIPE_CHUNKS] = {};
   cudaEvent_t pipe_done = nullptr;
   bool pipeline = true;  // pipelined staging of host arrays where the program allows it
+  // per-line exponent arrays of the FX links of the forward and adjoint
+  // programs (plan.cpp, link_fx; one per linked pass boundary)
+  std::vector<int*> lexp[2];
   // optional per-pass timing with CUDA events on the plan stream
   bool time_passes = false;
   std::vector<cudaEvent_t> pev;
@@ -210,5 +213,10 @@ int double_arith();
 void set_double_arith(int a);
 int plan_double_arith(const PlanDesc& d);
 long long pipelined_executes();  // executes through the host-array pipeline (plan.cpp)
+// FX mantissas kept between radix-8 passes of new double plans (plan.cpp):
+// on by default, PFFT_GB300_FX_LINK=0 or set_fx_link(0) turns it off
+int fx_link();
+void set_fx_link(int v);
+void unlink_fx(PassProgram* prog, std::vector<int*>* lexp);
 
 }  // namespace pg

@@ -193,6 +193,21 @@ bool fast_args(const PassParams& p, int arith, FastArgs* a, bool* row_in, bool* 
   a->mode = p.mode == MODE_C2C ? 0 : p.mode == MODE_R2C ? 1 : p.mode == MODE_C2R ? 2 : p.mode == MODE_RE10 ? 3 : 4;
   a->tw2 = nullptr;
   if (!fast_tables(p, arith, pow2, &a->tw, &a->tw2)) return false;
+  a->fx_in = arith == ARITH_F64 ? p.fx_in : 0;
+  a->fx_out = arith == ARITH_F64 ? p.fx_out : 0;
+  a->lexp_in = p.lexp_in;
+  a->lexp_out = p.lexp_out;
+  a->lexp_in_n = p.lexp_in_n;
+  for (int b = 0; b < PG_MAX_BATCH; b++) {
+    a->gin_np[b] = p.gin_np[b];
+    a->gin_bofs[b] = p.gin_bofs[b];
+  }
+  for (int q = 0; q < 2 * PG_MAX_BATCH; q++) {
+    a->gin_pext[q] = p.gin_pext[q];
+    a->gin_pcoef[q] = p.gin_pcoef[q];
+  }
+  a->gin_k = p.gin_k;
+  a->gout_off = p.gout_off;
   a->Zi = p.Zi;
   a->Ni = p.Ni;
   a->Zo = p.Zo;

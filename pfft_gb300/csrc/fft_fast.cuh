@@ -402,17 +402,23 @@ struct FX {
   static __device__ __forceinline__ C conj(C a) { return {a.x, -a.y}; }
   static __device__ __forceinline__ C lds(const S& s) { return {s.x, s.y}; }
   static __device__ __forceinline__ S sts(C v) { return make_longlong2(v.x, v.y); }
-  // floor(x * w / 2^64) up to a few units: x = xh 2^32 + xl, w = wh 2^32 + wl
-  // with signed low halves; the cross terms' high words and xh * wh.  With
-  // |x| < 2^62.5 and |w| < 2^62.5 the cross terms' high words are below 2^30
-  // each, so their sum is a 32-bit add.
+  // x * w / 2^64 rounded to the nearest unit, within 3/4 of a unit: x = xh
+  // 2^32 + xl, w = wh 2^32 + wl with signed low halves; xh * wh plus the two
+  // cross terms, summed exactly in 64 bits (|x|, |w| < 2^62.5 keep each
+  // below 2^61.5) and rounded once; the low-by-low part (below 1/4 of a
+  // unit, of either sign) is dropped.  Without a systematic loss no
+  // correction term is needed: 0 maps to 0, and errors do not pile up in
+  // one output bin (a floor's steady half unit would, in proportion to
+  // sqrt(N) of the result's norm).
   static __device__ __forceinline__ long long mh(long long x, int2 w) {
     const unsigned xu = (unsigned)x;
     const int xl = (int)xu;
     const int xh = (int)(x >> 32) + (int)(xu >> 31);
-    const int c = __mulhi(xh, w.y) + __mulhi(xl, w.x) + 1;
+    const long long s = (long long)xh * w.y + (long long)xl * w.x;
+    const int c = (int)(s >> 32) + (int)((unsigned)s >> 31);
     return (long long)xh * w.x + (long long)c;
   }
+  // Gauss's product: three rounded high products
   static __device__ __forceinline__ C mul(C a, const W& w) {
     const long long k1 = mh(a.x + a.y, w.r);
     const long long k2 = mh(a.x, w.d);
@@ -420,6 +426,7 @@ struct FX {
     return {k1 - k3, k1 + k2};
   }
   static __device__ __forceinline__ K8 c8() { return {}; }
+  // a * sqrt(1/2) = a - a (1 - sqrt(1/2)), the product rounded
   static __device__ __forceinline__ C scal(C a, K8) {
     const int2 k = make_int2(1257966796, 102865788);  // (1 - sqrt(1/2)) 2^64
     return {a.x - mh(a.x, k), a.y - mh(a.y, k)};
@@ -449,17 +456,29 @@ __device__ __forceinline__ long long fx_from_bits(long long b, int E) {
   const long long X = (long long)((m << 5) >> d);
   return b < 0 ? -X : X;
 }
-// Y * 2^eo rounded to the nearest double, as bits; eo == INT_MIN: NaN
+// Y * 2^eo rounded to the nearest double (ties away from zero); eo == INT_MIN:
+// NaN.  When every value of the tile lands in the normal range (-1022 <= eo
+// <= 960 with |Y| < 2^63, the same branch in every thread) the rounding is
+// branch-free: |Y| normalised by its leading-zero count, 53 bits kept plus
+// the next bit as the rounding increment, whose carry into bit 53 moves into
+// the exponent field by itself.
 __device__ __forceinline__ double fx_to_double(long long Y, int eo) {
+  if (eo >= -1022 && eo <= 960) {
+    const long long sg = Y >> 63;
+    const unsigned long long a = (unsigned long long)((Y ^ sg) - sg);
+    const int lz = __clzll((long long)a);
+    const unsigned long long n = a << (lz & 63);
+    const unsigned long long m = (n >> 11) + ((n >> 10) & 1ull);  // 2^52 <= m <= 2^53
+    const unsigned long long bits = ((unsigned long long)(eo + 1085 - lz) << 52) + m;
+    return __longlong_as_double(a ? (long long)(bits | ((unsigned long long)sg & 0x8000000000000000ull)) : 0ll);
+  }
   if (eo == INT_MIN) return __longlong_as_double(0x7FF8000000000000ll);
   const unsigned long long sgn = (unsigned long long)Y & 0x8000000000000000ull;
   const unsigned long long a = Y < 0 ? (unsigned long long)(-Y) : (unsigned long long)Y;
   if (a == 0) return 0.0;
   const int lz = __clzll((long long)a);
   const unsigned long long n = a << lz;  // bit 63 set
-  unsigned long long mant = n >> 11;
-  const unsigned rem = (unsigned)n & 0x7FFu;
-  mant += (rem > 0x400u || (rem == 0x400u && (mant & 1ull))) ? 1ull : 0ull;
+  unsigned long long mant = (n >> 11) + ((n >> 10) & 1ull);  // ties away, as the fast path
   int eb = eo + 1086 - lz;
   if (mant >> 53) {
     mant >>= 1;
@@ -498,6 +517,37 @@ __device__ __forceinline__ int fx_enter(FX::C (&v)[8], int conj_in) {
   return Eraw == 0x7FF ? INT_MIN : E - 1080;
 }
 
+// The tile's entry when its input holds FX mantissas of the previous pass
+// (fx_in): element r's value is v[r] * 2^ex[r], |v[r]| < 2^58 (stored
+// normalised, fx_store_normalise).  The new grid is 2^(max ex): the line with
+// the largest exponent keeps its mantissas, the others are shifted right to
+// it, rounded to nearest; an exponent INT_MAX (a previous tile that held an
+// infinity or NaN) makes the tile NaN.  Returns the exponent of the grid.
+__device__ __forceinline__ int fx_enter_linked(FX::C (&v)[8], const int (&ex)[8], int conj_in) {
+  __shared__ int red[32];
+  int em = ex[0];
+#pragma unroll
+  for (int r = 1; r < 8; r++) em = max(em, ex[r]);
+  em = __reduce_max_sync(0xffffffffu, em);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) red[warp] = em;
+  __syncthreads();
+  em = lane < (int)(blockDim.x >> 5) ? red[lane] : INT_MIN;
+  em = __reduce_max_sync(0xffffffffu, em);
+  if (em == INT_MAX) return INT_MIN;
+#pragma unroll
+  for (int r = 0; r < 8; r++) {
+    const int d = min(em - ex[r], 62);
+    if (d > 0) {
+      const long long h = 1ll << (d - 1);
+      v[r].x = (v[r].x + h) >> d;
+      v[r].y = (v[r].y + h) >> d;
+    }
+    if (conj_in) v[r].y = -v[r].y;
+  }
+  return em;
+}
+
 // Block normalisation of a stage (see FX): fx_ormag before the exchange's
 // barrier (each warp's OR of |high words| into slot[warp]), fx_normal_shift
 // after it (the tile's shift: the largest component below 2^60), fx_shift
@@ -516,14 +566,15 @@ __device__ __forceinline__ void fx_ormag_publish(unsigned m, unsigned* slot) {
   if ((threadIdx.x & 31) == 0) slot[threadIdx.x >> 5] = m;
 }
 // right shift (> 0) or left shift (< 0) bringing the bit length of the
-// tile's largest component to at most 60 (the OR of the high words gives it
+// tile's largest component to at most `bits` (60 before a stage, 58 for
+// mantissas stored for the next pass; the OR of the high words gives it
 // within one bit: an exact negative power of two reads one bit short)
-__device__ __forceinline__ int fx_normal_shift(const unsigned* slot) {
+__device__ __forceinline__ int fx_normal_shift(const unsigned* slot, int bits = 60) {
   const int lane = threadIdx.x & 31;
   unsigned m = lane < (int)(blockDim.x >> 5) ? slot[lane] : 0u;
   m = __reduce_or_sync(0xffffffffu, m);
   const int bl = 32 + (m ? 32 - __clz((int)m) : 0);
-  return bl - 59;
+  return bl - (bits - 1);
 }
 // x * 2^-s for -31 < s < 32, rounded to nearest (the same s in every thread:
 // no divergence)
@@ -544,6 +595,25 @@ __device__ __forceinline__ long long fx_shift(long long x, int s) {
 __device__ __forceinline__ unsigned* fx_slots() {
   __shared__ unsigned slots[2][32];  // per-warp ORs of two consecutive stages
   return &slots[0][0];
+}
+// Results kept for the next pass (fx_out): the tile renormalised so that its
+// largest component is below 2^58 (one more barrier); returns the shift to
+// add to the results' exponent.  slot: the parity the last exchange did not
+// use (every thread has passed its reads).
+template <int K>
+__device__ __forceinline__ int fx_store_normalise(FX::C (&v)[K], unsigned* slot) {
+  unsigned acc = 0;
+#pragma unroll
+  for (int r = 0; r < K; r++) {
+    const int hx = (int)(v[r].x >> 32), hy = (int)(v[r].y >> 32);
+    acc |= (unsigned)(hx ^ (hx >> 31)) | (unsigned)(hy ^ (hy >> 31));
+  }
+  fx_ormag_publish(acc, slot);
+  __syncthreads();
+  const int sh = fx_normal_shift(slot, 58);
+#pragma unroll
+  for (int r = 0; r < K; r++) v[r] = {fx_shift(v[r].x, sh), fx_shift(v[r].y, sh)};
+  return sh;
 }
 
 // Shared-memory layout of a tile: L lines at stride lsp_of, element p of a
@@ -610,6 +680,15 @@ struct FastArgs {
   int wmode;
   const void* tw2;
   int staged;  // host only: PassParams::staged
+  // FX mantissas kept between radix-8 passes (PassParams::fx_in / fx_out)
+  int fx_in, fx_out;
+  const int* lexp_in;
+  int* lexp_out;
+  long long lexp_in_n;
+  int gin_np[PG_MAX_BATCH];
+  long long gin_pext[2 * PG_MAX_BATCH], gin_pcoef[2 * PG_MAX_BATCH];
+  long long gin_bofs[PG_MAX_BATCH];
+  long long gin_k, gout_off;
 };
 
 // global element access: native format, or float-float pairs for the
@@ -675,6 +754,19 @@ __device__ __forceinline__ void gstore<FQ>(FDD::G* p, FDD::C v, int df) {
 template <>
 __device__ __forceinline__ void gstore<FX>(FX::G* p, FX::C v, int eo) {
   *p = make_double2(fx_to_double(v.x, eo), fx_to_double(v.y, eo));
+}
+
+// store of a complex result: FX with fx_out keeps the mantissas for the next
+// radix-8 pass (the line's exponent goes to lexp_out)
+template <class P>
+__device__ __forceinline__ void gput(const FastArgs& a, typename P::G* p, typename P::C v, int df) {
+  if constexpr (is_fx<P>()) {
+    if (a.fx_out) {
+      *(longlong2*)p = make_longlong2(v.x, v.y);
+      return;
+    }
+  }
+  gstore<P>(p, v, df);
 }
 
 // real-array element access (r2c input, c2r output)
@@ -804,7 +896,15 @@ __device__ __forceinline__ void store_elem(const FastArgs& a, long long off, int
   if (a.mode >= 2)
     rstore<P>(a.dst, off + (long long)k * a.sOa, v, eo);
   else
-    gstore<P>((typename P::G*)a.dst + off + (long long)k * a.sOa, v, is_fx<P>() ? eo : a.out_df);
+    gput<P>(a, (typename P::G*)a.dst + off + (long long)k * a.sOa, v, is_fx<P>() ? eo : a.out_df);
+}
+
+// bytes before the exchange area of a tile: the lines' input and output
+// offsets, and for FX the previous pass's line index of each line's element 0
+// (fx_in), rounded up to 16 bytes (one-line tiles of 4096 points)
+template <class P>
+__host__ __device__ constexpr int fast_hdr(int L) {
+  return is_fx<P>() ? (24 * L + 15) / 16 * 16 : 16 * L;  // the exchange area is 16-byte aligned
 }
 
 // ROW_IN: the axis is contiguous on the input side (thread t walks the line);
@@ -830,23 +930,35 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsi
   constexpr int TPL = N / 8;  // threads per line
   long long* offI = (long long*)sm_raw;
   long long* offO = offI + L;
-  S* buf = (S*)(sm_raw + 16 * L);
+  S* buf = (S*)(sm_raw + fast_hdr<P>(L));
 
   const int tid = threadIdx.x;
   const long long g0 = blk * L;
   if (tid < L) {
     long long g = g0 + tid;
     if (g >= a.nlines) g = a.nlines - 1;  // tail CTA: clamp (duplicate work, never stored)
-    long long oi = 0, oo = 0;
+    long long oi = 0, oo = 0, gi = 0;
+    int pc = 0;
     for (int b = 0; b < a.nb; b++) {
       long long e = a.bext[b];
       long long idx = g % e;
       g /= e;
       oi += idx * a.bsI[b];
       oo += idx * a.bsO[b];
+      if constexpr (is_fx<P>()) {
+        if (a.fx_in) {  // the previous pass's line index: this dimension's pieces
+          long long x = idx + a.gin_bofs[b];
+          for (int q = 0; q < a.gin_np[b]; q++, pc++) {
+            const long long ep = a.gin_pext[pc];
+            gi += (x % ep) * a.gin_pcoef[pc];
+            x /= ep;
+          }
+        }
+      }
     }
     offI[tid] = oi;
     offO[tid] = oo;
+    if constexpr (is_fx<P>()) offO[L + tid] = gi;  // fx_in: previous pass's line of element 0
   }
   __syncthreads();
   const int l = ROW_IN ? tid / TPL : tid % L;
@@ -891,7 +1003,15 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
   int sdf = a.out_df;  // FX: the results' exponent instead
   int fx_e = 0, fx_sh = 0;  // FX: the tile's grid exponent and the stages' shifts
   if constexpr (is_fx<P>()) {
-    fx_e = fx_enter<N>(v, IO == 0 ? a.conj_in : 0);  // IO 1: conjugated in load_elem
+    if (IO == 0 && a.fx_in) {  // mantissas of the previous radix-8 pass, each with its line's exponent
+      const long long gl = offO[L + l];
+      int ex[8];
+#pragma unroll
+      for (int r = 0; r < 8; r++) ex[r] = __ldg(a.lexp_in + min(gl + (long long)(t + r * TPL) * a.gin_k, a.lexp_in_n - 1));
+      fx_e = fx_enter_linked(v, ex, a.conj_in);
+    } else {
+      fx_e = fx_enter<N>(v, IO == 0 ? a.conj_in : 0);  // IO 1: conjugated in load_elem
+    }
     if constexpr (IO == 2) {
       if (a.mode == 4) {  // REDFT01: (x_k - i x_(N-k)) W_4N^-k, twiddles carrying 1/4
 #pragma unroll
@@ -929,7 +1049,11 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
     for (int r = 1; r < 8; r++) v[r] = P::mul(v[r], P::template twd<SIGN>(P::ldw(tw, Ns - 8 + (r - 1) * Ns + k, TWN)));
     bf8x<P, SIGN>(v);
   }
-  if constexpr (is_fx<P>()) sdf = fx_e == INT_MIN ? INT_MIN : fx_e + fx_sh;
+  if constexpr (is_fx<P>()) {
+    if (Q == 1 && a.fx_out) fx_sh += fx_store_normalise(v, fx_slots() + 32 * (NS8 & 1));
+    sdf = fx_e == INT_MIN ? INT_MIN : fx_e + fx_sh;
+    if (Q == 1 && a.fx_out && tid < L && g0 + tid < a.nlines) a.lexp_out[a.gout_off + g0 + tid] = sdf == INT_MIN ? INT_MAX : sdf;
+  }
   if (Q == 1) {
     // v holds the last stage (Ns = N/8, k = t): outputs y[t + r*TPL]
     if (ROW_IN == ROW_OUT) {
@@ -938,7 +1062,7 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
           G* dst = (G*)a.dst + offO[l] + (long long)t * a.sOa;
           const long long st = (long long)TPL * a.sOa;
 #pragma unroll
-          for (int r = 0; r < 8; r++) gstore<P>(dst + r * st, a.conj_out ? P::conj(v[r]) : v[r], sdf);
+          for (int r = 0; r < 8; r++) gput<P>(a, dst + r * st, a.conj_out ? P::conj(v[r]) : v[r], sdf);
         } else {
 #pragma unroll
           for (int r = 0; r < 8; r++) store_elem<P, IO == 2>(a, offO[l], t + r * TPL, v[r], N, sdf);
@@ -987,6 +1111,13 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
         bf4<P, SIGN>(w[b * Q], w[b * Q + 1], w[b * Q + 2], w[b * Q + 3]);
       }
     }
+    if constexpr (is_fx<P>()) {
+      if (a.fx_out) {
+        fx_sh += fx_store_normalise(w, fx_slots() + 32 * ((NS8 + 1) & 1));
+        sdf = fx_e == INT_MIN ? INT_MIN : fx_e + fx_sh;
+        if (tid < L && g0 + tid < a.nlines) a.lexp_out[a.gout_off + g0 + tid] = sdf == INT_MIN ? INT_MAX : sdf;
+      }
+    }
     if (ROW_IN == ROW_OUT) {
       if (live) {
         if constexpr (IO == 0) {
@@ -996,7 +1127,7 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
 #pragma unroll
             for (int r = 0; r < Q; r++) {
               C o = a.conj_out ? P::conj(w[b * Q + r]) : w[b * Q + r];
-              gstore<P>(dst + (long long)(t + b * TPL + r * NQ) * a.sOa, o, sdf);
+              gput<P>(a, dst + (long long)(t + b * TPL + r * NQ) * a.sOa, o, sdf);
             }
         } else {
 #pragma unroll
@@ -1027,7 +1158,7 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
         C o = P::lds(line2[pad<P>(k)]);
         if constexpr (IO == 0) {
           if (a.conj_out) o = P::conj(o);
-          gstore<P>(d2 + (long long)k * a.sOa, o, sdf);
+          gput<P>(a, d2 + (long long)k * a.sOa, o, sdf);
         } else {
           store_elem<P, IO == 2>(a, offO[l2], k, o, N, sdf);
         }
@@ -1051,7 +1182,7 @@ __global__ void __launch_bounds__(L*(N / 8), (fast_min_blocks<P, L*(N / 8)>())) 
 
 template <class P, int N, int L>
 constexpr size_t fast_smem_bytes() {
-  return 16 * L + (size_t)L * (sizeof(typename P::S) == 8 ? N + 16 : N + N / 8 + 4) * sizeof(typename P::S);
+  return fast_hdr<P>(L) + (size_t)L * (sizeof(typename P::S) == 8 ? N + 16 : N + N / 8 + 4) * sizeof(typename P::S);
 }
 
 // ---- staged persistent variant (plain c2c passes) ---------------------------

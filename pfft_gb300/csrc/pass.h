@@ -113,6 +113,23 @@ struct PassParams {
   int fastL;    // radix-8 kernel lines per CTA (0: default for the length)
   int staged;   // staged variant of the radix-8 kernel (plain c2c passes): 0 default
                 // (float column passes), 1 on where the layout allows, 2 off
+  // double plans, 64-bit fixed point kept between two radix-8 passes (FX):
+  // fx_out stores the mantissas (int64 pairs, the 16 bytes of a complex
+  // double) and one exponent per line into lexp_out[gout_off + line]; fx_in
+  // reads them, the exponent of an element being that of its line in the
+  // previous pass: lexp_in[sum over this pass's batch dimensions b of the
+  // pieces of (idx_b + gin_bofs[b]) + k * gin_k], k the position along this
+  // pass's axis.  Batch dimension b is split into gin_np[b] pieces (mixed
+  // radix, fastest first, extents gin_pext, coefficients gin_pcoef, listed
+  // dimension after dimension): the previous pass's dimensions it crosses.
+  int fx_in, fx_out;
+  const int* lexp_in;
+  int* lexp_out;
+  long long lexp_in_n;  // entries of lexp_in (bound of every lookup)
+  int gin_np[PG_MAX_BATCH];
+  long long gin_pext[2 * PG_MAX_BATCH], gin_pcoef[2 * PG_MAX_BATCH];
+  long long gin_bofs[PG_MAX_BATCH];
+  long long gin_k, gout_off;
   int quant;    // double API, plain c2c passes of the radix-8 and mixed-radix
                 // kernels: float-float plans (ARITH_DF) with block-quantised high
                 // words (1) instead of TwoSum additions (0); double plans

@@ -96,6 +96,129 @@ static void mark_quant(const Plan* pl, PassProgram* prog) {
   for (Pass& ps : prog->passes) ps.p.quant = pl->quant;
 }
 
+// FX mantissas kept between two consecutive radix-8 passes of a default
+// double plan (PassParams::fx_out / fx_in): the first pass stores its int64
+// mantissas and one exponent per line, the second reads them and aligns each
+// element to its tile's grid, so neither converts to or from double.  The
+// second pass must be a plain c2c pass, the first any radix-8 pass with a
+// complex output; the second pass's input dimensions are matched to the first
+// pass's output dimensions by stride and extent, which gives the previous
+// pass's line index of each element (PassParams::gin_np, gin_pext, gin_pcoef, gin_k).
+static int g_fx_link = -1;
+int fx_link() {
+  if (g_fx_link < 0) {
+    const char* e = getenv("PFFT_GB300_FX_LINK");
+    g_fx_link = (e && strcmp(e, "0") == 0) ? 0 : 1;
+  }
+  return g_fx_link;
+}
+void set_fx_link(int v) { g_fx_link = v ? 1 : 0; }
+
+void unlink_fx(PassProgram* prog, std::vector<int*>* lexp) {
+  for (int* q : *lexp)
+    if (q) cudaFree(q);
+  lexp->clear();
+  for (Pass& ps : prog->passes) {
+    PassParams& p = ps.p;
+    p.fx_in = p.fx_out = 0;
+    p.lexp_in = nullptr;
+    p.lexp_out = nullptr;
+    p.lexp_in_n = 0;
+    for (int b = 0; b < PG_MAX_BATCH; b++) p.gin_np[b] = 0, p.gin_bofs[b] = 0;
+    for (int q = 0; q < 2 * PG_MAX_BATCH; q++) p.gin_pext[q] = 1, p.gin_pcoef[q] = 0;
+    p.gin_k = p.gout_off = 0;
+  }
+}
+
+static bool link_fx(Plan* pl, PassProgram* prog, std::vector<int*>* lexp) {
+  unlink_fx(prog, lexp);
+  const int P = (int)prog->passes.size();
+  if (pl->arith != ARITH_F64 || pl->quant != 2 || !fx_link() || P < 2) return true;
+  lexp->assign(P, nullptr);
+  for (int i = 0; i + 1 < P; i++) {
+    PassParams& a = prog->passes[i].p;
+    PassParams& b = prog->passes[i + 1].p;
+    const bool b_plain = b.mode == MODE_C2C && b.Zi == 0 && b.Ni == b.N && b.Zo == 0 && b.No == b.N && !b.wmode;
+    if (!b_plain || (a.mode != MODE_C2C && a.mode != MODE_R2C)) continue;
+    if (!fast_pass_eligible(a, pl->arith) || !fast_pass_eligible(b, pl->arith)) continue;
+    // b's input dimensions onto a's output dimensions.  Both passes' planner
+    // merged dimensions contiguous on both of their sides, so one of b's
+    // dimensions may cross several of a's, or lie inside one: it is cut into
+    // pieces at a's dimension boundaries (walking its strides upward), each
+    // piece contributing its coordinate times a's line-index weight for it
+    // (0 inside a's axis).
+    struct ADim {
+      long long s, e, w;  // stride, extent, line-index weight per unit of coordinate
+    };
+    std::vector<ADim> ad;
+    long long Mj = 1;
+    for (int j = 0; j < a.nb; j++) {
+      ad.push_back({a.bsO[j], a.bext[j], Mj});
+      Mj *= a.bext[j];
+    }
+    ad.push_back({a.sOa, a.No, 0});
+    bool ok = true;
+    std::vector<long long> pe, pc;  // pieces of the current dimension
+    auto pieces = [&](long long ext, long long stride) {
+      pe.clear();
+      pc.clear();
+      long long cur = stride, rem = ext;
+      while (rem > 1 && ok) {
+        const ADim* hit = nullptr;
+        for (const ADim& x : ad)
+          if (x.s > 0 && x.e > 1 && cur % x.s == 0 && cur / x.s < x.e) hit = &x;
+        if (!hit) {
+          ok = false;
+          break;
+        }
+        const long long m = cur / hit->s;            // position inside a's dimension
+        if (hit->e % m) ok = false;
+        const long long room = hit->e / m;           // extent left in a's dimension
+        const long long p = std::min(rem, room);
+        if (rem % p || (p < rem && p != room)) ok = false;
+        pe.push_back(p);
+        pc.push_back(hit->w * m);
+        cur *= p;
+        rem /= p;
+      }
+    };
+    int np[PG_MAX_BATCH] = {0};
+    long long pext[2 * PG_MAX_BATCH], pcoef[2 * PG_MAX_BATCH];
+    int npc = 0;
+    for (int d = 0; d < b.nb && ok; d++) {
+      pieces(b.bext[d], b.bsI[d]);
+      if (npc + (int)pe.size() > 2 * PG_MAX_BATCH) ok = false;
+      for (size_t q = 0; ok && q < pe.size(); q++, npc++) {
+        pext[npc] = pe[q];
+        pcoef[npc] = pc[q];
+      }
+      np[d] = (int)pe.size();
+    }
+    long long gk = 0;
+    if (ok) {
+      pieces(b.N, b.sIa);  // the axis: one piece (a per-element coefficient)
+      if (pe.size() > 1) ok = false;
+      if (pe.size() == 1) gk = pc[0];
+    }
+    if (!ok) continue;
+    int* q = nullptr;
+    if (cuda_check(cudaMalloc(&q, sizeof(int) * (size_t)a.nlines), "line exponents")) return false;
+    (*lexp)[i] = q;
+    a.fx_out = 1;
+    a.lexp_out = q;
+    b.fx_in = 1;
+    b.lexp_in = q;
+    b.lexp_in_n = a.nlines;
+    for (int d = 0; d < PG_MAX_BATCH; d++) b.gin_np[d] = d < b.nb ? np[d] : 0;
+    for (int x = 0; x < npc; x++) {
+      b.gin_pext[x] = pext[x];
+      b.gin_pcoef[x] = pcoef[x];
+    }
+    b.gin_k = gk;
+  }
+  return true;
+}
+
 // ---- plans -------------------------------------------------------------------
 bool ensure_workspace(Plan* pl, const PassProgram& prog) {
   for (int k = 0; k < 2; k++) {
@@ -181,6 +304,10 @@ Plan* make_plan(const PlanDesc& base, void* in, void* out) {
     destroy_plan(pl);
     return nullptr;
   }
+  if (!link_fx(pl, &pl->fwd, &pl->lexp[0])) {
+    destroy_plan(pl);
+    return nullptr;
+  }
   // pre-build twiddle tables so that execution allocates nothing
   for (const Pass& ps : pl->fwd.passes) {
     cudaError_t e;
@@ -214,6 +341,8 @@ void destroy_plan(Plan* pl) {
       if (pl->pipe_ev[k][c]) cudaEventDestroy(pl->pipe_ev[k][c]);
   }
   if (pl->pipe_done) cudaEventDestroy(pl->pipe_done);
+  unlink_fx(&pl->fwd, &pl->lexp[0]);
+  unlink_fx(&pl->adj, &pl->lexp[1]);
   delete pl;
 }
 
@@ -289,6 +418,10 @@ static PassParams chunk_of(const PassParams& p, int arith, int k, int C) {
   q.dst = (char*)p.dst + a * p.bsO[b] * pass_esz(p, arith, false);
   q.bshI[b].start += (int)a;
   q.bshO[b].start += (int)a;
+  // FX line indices of the slab: its coordinates along b start at a, its
+  // lines are global lines k * nlines/C on
+  q.gin_bofs[b] = p.gin_bofs[b] + a;
+  q.gout_off = p.gout_off + (long long)k * q.nlines;
   return q;
 }
 
@@ -388,6 +521,7 @@ static int run_pipelined(Plan* pl, const PassProgram& prog, void* in, void* out,
       q.src = (const char*)p.src + (size_t)j * (size_t)(p.bext[0] / C) * (size_t)p.bsI[0] * pass_esz(p, pl->arith, true);
       q.bshI[0].start += (int)(j * (p.bext[0] / C));
       q.bshO[0].start += (int)(j * (p.bext[0] / C));
+      q.gin_bofs[0] = p.gin_bofs[0] + (long long)j * (p.bext[0] / C);  // (the last pass stores doubles)
       rc = launch_prog_pass(pl, ps, q, s);
       if (rc) {
         cuda_check((cudaError_t)rc, "pass launch");
@@ -423,6 +557,7 @@ void execute_plan(Plan* pl, void* in, void* out, bool adjoint) {
     if (!ensure_workspace(pl, pl->adj)) return;
     apply_wisdom(&pl->adj, pl->arith);
     if ((pl->d.pfft_flags & (F_PATIENT | F_EXHAUSTIVE | F_TUNE)) && !tune_program(pl, &pl->adj)) return;
+    if (!link_fx(pl, &pl->adj, &pl->lexp[1])) return;
     pl->adj_built = true;
   }
   const PassProgram& prog = adjoint ? pl->adj : pl->fwd;

@@ -124,3 +124,48 @@ def test_fx_large_transform_against_oracle(cuda, pfft_lib):
     e_fx = rel_l2(gpu_run(req, x, prec="double"), ref)
     e_nat = rel_l2(gpu_run(req, x, prec="double-f64"), ref)
     assert e_fx <= 1e-15 and e_fx <= 1.25 * e_nat, (e_fx, e_nat)
+
+
+@pytest.mark.parametrize("link", [0, 1])
+@pytest.mark.parametrize("req", [Req("c2c", (32, 64, 128)), Req("c2c", (32, 64, 128), flags=pg.PFFT_TRANSPOSED_OUT),
+                                 Req("c2c", (16, 32, 64), sign=1, flags=pg.PFFT_TRANSPOSED_IN),
+                                 Req("c2c", (8, 16, 32, 64)), Req("c2c", (16, 32, 64), howmany=3),
+                                 Req("r2c", (32, 64, 128), flags=pg.PFFT_PADDED_R2C | pg.PFFT_TRANSPOSED_OUT),
+                                 Req("c2r", (32, 64, 128), sign=1)],
+                         ids=["c2c", "c2c_to", "c2c_ti_bwd", "c2c_4d", "c2c_hm3", "r2c_pad_to", "c2r"])
+def test_fx_mantissas_between_passes(cuda, pfft_lib, req, link):
+    """Mode 2 keeps the int64 mantissas and one exponent per line between two
+    radix-8 passes (pfft_gb300_set_fx_link, on by default) instead of
+    rounding to double in between: with and without, every layout matches the
+    oracle at FP64 level."""
+    L = pfft_lib
+    old = L.pfft_gb300_set_fx_link(link)
+    try:
+        x = random_input(req, np.random.default_rng(31))
+        ref = oracle_run(req, x)
+        got = gpu_run(req, x, prec="double")
+    finally:
+        L.pfft_gb300_set_fx_link(old)
+    from tests.pfft_util import mask_padding
+    assert rel_l2(mask_padding(req, got), mask_padding(req, ref)) <= 1e-15
+
+
+@pytest.mark.parametrize("n,flags,links", [((512, 64, 128), 0, [2, 3, 1]), ((32, 64, 128), pg.PFFT_TRANSPOSED_OUT, [2, 3, 1]),
+                                           ((16, 16, 32, 64), 0, [2, 3, 3, 1]), ((64, 48, 32), 0, [0, 0, 0])])
+def test_fx_links_form(cuda, pfft_lib, n, flags, links):
+    """Consecutive power-of-two c2c passes of a default double plan keep the
+    mantissas between them (1 = input linked, 2 = output linked); a
+    non-power-of-two axis (48, general kernel in FP64) breaks the chain."""
+    torch = cuda
+    L = pfft_lib
+    cnt = int(np.prod(n))
+    a = torch.zeros(2 * cnt, dtype=torch.float64, device="cuda")
+    b = torch.zeros_like(a)
+    p = L.pfft_plan_dft(len(n), pg.ints(n), a.data_ptr(), b.data_ptr(), pg.procmesh(2), pg.PFFT_FORWARD, flags)
+    assert p, pg.last_error()
+    got = [L.pfft_gb300_pass_fx_link(p, i) for i in range(len(links))]
+    L.pfft_destroy_plan(p)
+    if 48 in n:  # the 48-point pass breaks the chain on both sides
+        assert got[1] == 0
+    else:
+        assert got == links
