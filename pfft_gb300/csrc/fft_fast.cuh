@@ -387,10 +387,12 @@ struct FX {
   struct C {
     long long x, y;
   };
-  // twiddle w / 4 (stored as (hi, lo) with lo in [-2^31, 2^31), value hi * 2^32
-  // + lo, scaled by 2^64): r = Re w, d = Im w - Re w, s = Re w + Im w
+  // twiddle w / 4 = c + i s scaled by 2^64, each part stored as (hi, lo),
+  // value hi * 2^32 + lo with lo in [-2^31, 2^31): a = (c.hi, c.lo, s.hi,
+  // s.lo), n = -s (split on its own, so no negation can overflow)
   struct W {
-    int2 r, d, s;
+    int4 a;
+    int2 n;
   };
   struct K8 {};  // tag of the sqrt(1/2) constant
   static __device__ __forceinline__ C add(C a, C b) { return {a.x + b.x, a.y + b.y}; }
@@ -418,12 +420,22 @@ struct FX {
     const int c = (int)(s >> 32) + (int)((unsigned)s >> 31);
     return (long long)xh * w.x + (long long)c;
   }
-  // Gauss's product: three rounded high products
+  // (x + i y) (c + i s) / 2^64, each part rounded once: with x = xh 2^32 +
+  // xl and y, c, s split alike, Re = xh ch - yh sh + round(m / 2^32), m = xh
+  // cl + xl ch - yh sl - yl sh (exact in 64 bits: |x|, |y| < 2^60 and |c|,
+  // |s| <= 2^62 keep each term below 2^61), Im alike; the low-by-low terms
+  // (below 1/2 of a unit together) are dropped.  Twelve 32x32->64-bit
+  // multiply-adds and a few integer adds per product, within 1 unit.
   static __device__ __forceinline__ C mul(C a, const W& w) {
-    const long long k1 = mh(a.x + a.y, w.r);
-    const long long k2 = mh(a.x, w.d);
-    const long long k3 = mh(a.y, w.s);
-    return {k1 - k3, k1 + k2};
+    const unsigned xu = (unsigned)a.x, yu = (unsigned)a.y;
+    const int xl = (int)xu, yl = (int)yu;
+    const int xh = (int)(a.x >> 32) + (int)(xu >> 31), yh = (int)(a.y >> 32) + (int)(yu >> 31);
+    const long long rm = (long long)xh * w.a.y + (long long)xl * w.a.x + (long long)yh * w.n.y + (long long)yl * w.n.x;
+    const long long im = (long long)xh * w.a.w + (long long)xl * w.a.z + (long long)yh * w.a.y + (long long)yl * w.a.x;
+    const int rc = (int)(rm >> 32) + (int)((unsigned)rm >> 31);
+    const int ic = (int)(im >> 32) + (int)((unsigned)im >> 31);
+    return {(long long)xh * w.a.x + (long long)yh * w.n.x + (long long)rc,
+            (long long)xh * w.a.z + (long long)yh * w.a.x + (long long)ic};
   }
   static __device__ __forceinline__ K8 c8() { return {}; }
   // a * sqrt(1/2) = a - a (1 - sqrt(1/2)), the product rounded
@@ -434,8 +446,8 @@ struct FX {
   // element 0 of a twiddled stage (twiddle 1, scaled by 1/4, rounded to nearest)
   static __device__ __forceinline__ C tw0(C a) { return {(a.x + 2) >> 2, (a.y + 2) >> 2}; }
   static __device__ __forceinline__ W ldw(const void* base, int idx, int cnt) {
-    const int2* t = (const int2*)base;
-    return {__ldg(t + idx), __ldg(t + cnt + idx), __ldg(t + 2 * cnt + idx)};
+    const int4* t = (const int4*)base;
+    return {__ldg(t + idx), __ldg((const int2*)(t + cnt) + idx)};
   }
   template <int SIGN>
   static __device__ __forceinline__ W twd(const W& w) {

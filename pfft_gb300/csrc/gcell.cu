@@ -207,59 +207,149 @@ __global__ void __launch_bounds__(GC_THREADS) k_gc_move(T* __restrict__ data, co
   }
 }
 
+// k mod n in [0, n); one compare for the usual |k| < 2n
 __device__ __forceinline__ long long gc_wrap(long long k, long long n) {
-  long long j = k % n;
+  if (k >= 0 && k < n) return k;
+  if (k < 0 && k >= -n) return k + n;
+  if (k >= n && k < 2 * n) return k - n;
+  const long long j = k % n;
   return j < 0 ? j + n : j;
 }
 
-// every ghost cell of the box <- its interior image (one warp per box row)
+// Work lists of the fill and the fold (host-computed counts).  Part A: rows
+// of which only a few cells along axis 2 take part (per scalars each), rpw
+// rows to a warp, a lane to a scalar; part B: rows of which every cell takes
+// part, a warp to a row.  Row-internal indexes are 32-bit: a row of the
+// single-sweep path holds at most 8192 scalars.
+struct GcWork {
+  long long rowsA, rowsB;
+  int per, rpw;
+};
+
+// every ghost cell of the box <- its interior image.  Part A: the ghost cells
+// at both ends of every interior row (k0, k1 inside the block); part B: the
+// ghost rows (k0 or k1 outside), enumerated as the ghost planes along axis 0
+// and then the ghost rows of the interior planes.  Both read interior cells
+// only, which neither writes.
 template <class T>
-__global__ void __launch_bounds__(GC_THREADS) k_gc_fill(T* __restrict__ data, GcDims g, long long nrows) {
+__global__ void __launch_bounds__(GC_THREADS) k_gc_fill(T* __restrict__ data, GcDims g, GcWork w) {
   const int lane = threadIdx.x & 31;
   const long long warps = (long long)gridDim.x * (GC_THREADS / 32);
-  const long long tu = g.tuple, RB = g.ng[2] * tu, gb2t = g.gb[2] * tu, endt = (g.gb[2] + g.n[2]) * tu;
-  for (long long b = (long long)blockIdx.x * (GC_THREADS / 32) + (threadIdx.x >> 5); b < nrows; b += warps) {
-    const long long k0 = b / g.ng[1], k1 = b - k0 * g.ng[1];
-    const bool interior = k0 >= g.gb[0] && k0 < g.gb[0] + g.n[0] && k1 >= g.gb[1] && k1 < g.gb[1] + g.n[1];
-    const long long j0 = gc_wrap(k0 - g.gb[0], g.n[0]), j1 = gc_wrap(k1 - g.gb[1], g.n[1]);
-    const T* src = data + ((j0 + g.gb[0]) * g.ng[1] + j1 + g.gb[1]) * RB;
-    T* dst = data + b * RB;
-    // interior rows: the cells before and after the interior; ghost rows: all
-    const long long cnt = interior ? RB - (endt - gb2t) : RB;
-    for (long long s = lane; s < cnt; s += 32) {
-      const long long t = (interior && s >= gb2t) ? s + (endt - gb2t) : s;  // scalar of the box row
-      const long long k2 = t / tu, h = t - k2 * tu;
-      dst[t] = src[(gc_wrap(k2 - g.gb[2], g.n[2]) + g.gb[2]) * tu + h];
+  const long long n0 = g.n[0], n1 = g.n[1], n2 = g.n[2], gb0 = g.gb[0], gb1 = g.gb[1], gb2 = g.gb[2];
+  const long long ng1 = g.ng[1], e0 = g.ng[0] - n0, e1 = ng1 - n1;
+  const unsigned tu = (unsigned)g.tuple, RB = (unsigned)(g.ng[2] * g.tuple);
+  const long long groupsA = (w.rowsA + w.rpw - 1) / w.rpw;
+  const int lr = w.rpw > 1 ? lane / w.per : 0, lc0 = w.rpw > 1 ? lane % w.per : lane;
+  for (long long q = (long long)blockIdx.x * (GC_THREADS / 32) + (threadIdx.x >> 5); q < groupsA + w.rowsB; q += warps) {
+    if (q < groupsA) {
+      const long long row = q * w.rpw + lr;
+      if (lr >= w.rpw || row >= w.rowsA) continue;
+      const long long j0 = row / n1, j1 = row - j0 * n1;
+      T* base = data + ((j0 + gb0) * ng1 + j1 + gb1) * RB;
+      for (int lc = lc0; lc < w.per; lc += 32) {
+        const unsigned c = (unsigned)lc / tu, h = (unsigned)lc - c * tu;
+        const long long k2 = c < gb2 ? c : c + n2;
+        base[k2 * tu + h] = base[(gc_wrap(k2 - gb2, n2) + gb2) * tu + h];
+      }
+    } else {
+      const long long r = q - groupsA, planes = e0 * ng1;
+      long long k0, k1;
+      if (r < planes) {
+        const long long p = r / ng1;
+        k1 = r - p * ng1;
+        k0 = p < gb0 ? p : p + n0;
+      } else {
+        const long long p = (r - planes) / e1, c = r - planes - p * e1;
+        k0 = gb0 + p;
+        k1 = c < gb1 ? c : c + n1;
+      }
+      const T* src = data + ((gc_wrap(k0 - gb0, n0) + gb0) * ng1 + gc_wrap(k1 - gb1, n1) + gb1) * RB;
+      T* dst = data + (k0 * ng1 + k1) * RB;
+      for (unsigned t = lane; t < RB; t += 32) {
+        const unsigned k2 = t / tu, h = t - k2 * tu;
+        dst[t] = src[(gc_wrap((long long)k2 - gb2, n2) + gb2) * tu + h];
+      }
     }
   }
 }
 
-// every block cell with more than one image <- the sum of its images
-// (k0, k1, k2 ascending), written at its interior position (one warp per
-// block row)
+// every block cell with more than one image <- the sum of its images (k0,
+// k1, k2 ascending), written at its interior position.  A cell j has the
+// images s, s + n, ... below ng per axis, s = (j + gb) mod n: more than one
+// for s < m = min(ng - n, n).  Part A: the rows with one image along axes 0
+// and 1 (s0 >= m0, s1 >= m1; then k0 = s0, k1 = s1 is the interior row),
+// their cells s2 < m2; part B: the rows with s0 < m0 or s1 < m1, all cells.
+// A thread reads only its own cell's images, so the in-place sums do not
+// race.
 template <class T>
-__global__ void __launch_bounds__(GC_THREADS) k_gc_fold(T* __restrict__ data, GcDims g, long long nrows) {
+__global__ void __launch_bounds__(GC_THREADS) k_gc_fold(T* __restrict__ data, GcDims g, GcWork w) {
   const int lane = threadIdx.x & 31;
   const long long warps = (long long)gridDim.x * (GC_THREADS / 32);
-  const long long tu = g.tuple;
-  for (long long r = (long long)blockIdx.x * (GC_THREADS / 32) + (threadIdx.x >> 5); r < nrows; r += warps) {
-    const long long j0 = r / g.n[1], j1 = r - j0 * g.n[1];
-    const long long s0 = (j0 + g.gb[0]) % g.n[0], s1 = (j1 + g.gb[1]) % g.n[1];
-    const bool many01 = s0 + g.n[0] < g.ng[0] || s1 + g.n[1] < g.ng[1];
-    for (long long j2 = lane; j2 < g.n[2]; j2 += 32) {
-      const long long s2 = (j2 + g.gb[2]) % g.n[2];
-      if (!many01 && s2 + g.n[2] >= g.ng[2]) continue;  // a single image: nothing to add
-      const long long at = (((j0 + g.gb[0]) * g.ng[1] + j1 + g.gb[1]) * g.ng[2] + j2 + g.gb[2]) * tu;
-      for (long long h = 0; h < tu; h++) {
+  const long long n0 = g.n[0], n1 = g.n[1], n2 = g.n[2], gb0 = g.gb[0], gb1 = g.gb[1], gb2 = g.gb[2];
+  const long long ng0 = g.ng[0], ng1 = g.ng[1], ng2 = g.ng[2];
+  const long long m0 = ng0 - n0 < n0 ? ng0 - n0 : n0, m1 = ng1 - n1 < n1 ? ng1 - n1 : n1;
+  const unsigned tu = (unsigned)g.tuple, RB = (unsigned)(ng2 * g.tuple);
+  const long long groupsA = (w.rowsA + w.rpw - 1) / w.rpw;
+  const int lr = w.rpw > 1 ? lane / w.per : 0, lc0 = w.rpw > 1 ? lane % w.per : lane;
+  for (long long q = (long long)blockIdx.x * (GC_THREADS / 32) + (threadIdx.x >> 5); q < groupsA + w.rowsB; q += warps) {
+    if (q < groupsA) {
+      const long long row = q * w.rpw + lr;
+      if (lr >= w.rpw || row >= w.rowsA) continue;
+      const long long a0 = row / (n1 - m1);
+      T* rowp = data + ((m0 + a0) * ng1 + m1 + row - a0 * (n1 - m1)) * RB;
+      for (int lc = lc0; lc < w.per; lc += 32) {
+        const unsigned s2 = (unsigned)lc / tu, h = (unsigned)lc - s2 * tu;
         T acc = 0;
-        for (long long k0 = s0; k0 < g.ng[0]; k0 += g.n[0])
-          for (long long k1 = s1; k1 < g.ng[1]; k1 += g.n[1])
-            for (long long k2 = s2; k2 < g.ng[2]; k2 += g.n[2])
-              acc += data[((k0 * g.ng[1] + k1) * g.ng[2] + k2) * tu + h];
-        data[at + h] = acc;
+        for (long long k2 = s2; k2 < ng2; k2 += n2) acc += rowp[k2 * tu + h];
+        rowp[(gc_wrap(s2 - gb2, n2) + gb2) * tu + h] = acc;
+      }
+    } else {
+      const long long r = q - groupsA;
+      long long s0, s1;
+      if (r < m0 * n1) {
+        s0 = r / n1;
+        s1 = gc_wrap(r - s0 * n1 + gb1, n1);
+      } else {
+        const long long p = (r - m0 * n1) / m1;
+        s0 = m0 + p;
+        s1 = r - m0 * n1 - p * m1;
+      }
+      T* at = data + ((gc_wrap(s0 - gb0, n0) + gb0) * ng1 + gc_wrap(s1 - gb1, n1) + gb1) * RB;
+      for (unsigned t = lane; t < (unsigned)(n2 * tu); t += 32) {
+        const unsigned j2 = t / tu, h = t - j2 * tu;
+        const long long s2 = gc_wrap(j2 + gb2, n2);
+        T acc = 0;
+        for (long long k0 = s0; k0 < ng0; k0 += n0)
+          for (long long k1 = s1; k1 < ng1; k1 += n1)
+            for (long long k2 = s2; k2 < ng2; k2 += n2) acc += data[((k0 * ng1 + k1) * ng2 + k2) * tu + h];
+        at[(j2 + gb2) * tu + h] = acc;
       }
     }
   }
+}
+
+// fill: part A the interior rows' end cells, part B the ghost rows
+GcWork gc_fill_work(const GcDims& g) {
+  GcWork w;
+  const long long e2 = g.ng[2] - g.n[2];
+  w.per = (int)(e2 * g.tuple);
+  w.rowsA = w.per > 0 ? g.n[0] * g.n[1] : 0;
+  w.rowsB = (g.ng[0] - g.n[0]) * g.ng[1] + g.n[0] * (g.ng[1] - g.n[1]);
+  w.rpw = w.per > 0 && w.per <= 16 ? 32 / w.per : 1;
+  if (w.per == 0) w.per = 1;
+  return w;
+}
+// fold: part A the single-image rows' cells s2 < m2, part B the other rows
+GcWork gc_fold_work(const GcDims& g) {
+  GcWork w;
+  const long long m0 = std::min(g.ng[0] - g.n[0], g.n[0]), m1 = std::min(g.ng[1] - g.n[1], g.n[1]);
+  const long long m2 = std::min(g.ng[2] - g.n[2], g.n[2]);
+  w.per = (int)(m2 * g.tuple);
+  w.rowsA = w.per > 0 ? (g.n[0] - m0) * (g.n[1] - m1) : 0;
+  w.rowsB = m0 * g.n[1] + (g.n[0] - m0) * m1;
+  w.rpw = w.per > 0 && w.per <= 16 ? 32 / w.per : 1;
+  if (w.per == 0) w.per = 1;
+  return w;
 }
 
 struct GcPlan {
@@ -437,8 +527,9 @@ int gc_exchange_t(GcPlan* p, void* data) {
   }
   int rc = gc_move<T, true>(p, data);
   if (rc) return rc;
-  const long long rows = p->g.ng[0] * p->g.ng[1];
-  k_gc_fill<T><<<gc_rows_grid(p, rows), GC_THREADS, 0, p->stream>>>((T*)data, p->g, rows);
+  const GcWork w = gc_fill_work(p->g);
+  const long long units = (w.rowsA + w.rpw - 1) / w.rpw + w.rowsB;
+  if (units > 0) k_gc_fill<T><<<gc_rows_grid(p, units), GC_THREADS, 0, p->stream>>>((T*)data, p->g, w);
   return (int)cudaGetLastError();
 }
 
@@ -452,8 +543,9 @@ int gc_reduce_t(GcPlan* p, void* data) {
     if (e != cudaSuccess) return (int)e;
     k_gc_reduce<T><<<launch_grid(p->ncomp), 256, 0, p->stream>>>((const T*)p->scratch, (T*)data, p->g, p->ncomp);
   } else {
-    const long long rows = p->g.n[0] * p->g.n[1];
-    k_gc_fold<T><<<gc_rows_grid(p, rows), GC_THREADS, 0, p->stream>>>((T*)data, p->g, rows);
+    const GcWork w = gc_fold_work(p->g);
+    const long long units = (w.rowsA + w.rpw - 1) / w.rpw + w.rowsB;
+    if (units > 0) k_gc_fold<T><<<gc_rows_grid(p, units), GC_THREADS, 0, p->stream>>>((T*)data, p->g, w);
     e = cudaGetLastError();
     if (e != cudaSuccess) return (int)e;
     int rc = gc_move<T, false>(p, data);

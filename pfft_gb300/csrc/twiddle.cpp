@@ -109,12 +109,12 @@ const void* twiddle_table(int M, int arith, cudaError_t* err) {
     s = -s;  // forward direction
     if (fx) {
       if (bwd) s = -s;
-      const long double v[3] = {c, s - c, c + s};
-      for (int q = 0; q < 3; q++) {
-        int hl[2];
-        fx_split(v[q], hl);
-        memcpy(&host[(q * n + j) * 8], hl, 8);
-      }
+      int a[4], ns[2];
+      fx_split(c, a);
+      fx_split(s, a + 2);
+      fx_split(-s, ns);
+      memcpy(&host[j * 16], a, 16);
+      memcpy(&host[n * 16 + j * 8], ns, 8);
     } else if (packed) {
       if (bwd) s = -s;
       float h[4], l[4];
