@@ -624,6 +624,8 @@ def main():
                          "pass's candidates at planning time, before the timed region)")
     ap.add_argument("--batched-only", default=None, choices=["double", "float"],
                     help="print only the batched-vs-loop measurement of that precision (profiling runs)")
+    ap.add_argument("--halo-only", action="store_true",
+                    help="print only the 256^3 halo exchange / reduce measurement (profiling runs)")
     ap.add_argument("--prec", default="double", choices=["double", "float"],
                     help="double = pfft_ (complex128, the headline); float = pfftf_ (complex64)")
     args = ap.parse_args()
@@ -639,6 +641,9 @@ def main():
     L = pg.lib()
     if args.batched_only:
         print(json.dumps(measure_batched(L, pg, torch, args.batched_only, tune=not args.no_tune)), flush=True)
+        return
+    if args.halo_only:
+        print(json.dumps(measure_halo(L, pg, torch, measured_peak())), flush=True)
         return
     dev = torch.device("cuda", local)
     n = tuple(int(v) for v in args.shape.split("x")) if args.shape else (args.n, args.n, args.n)

@@ -139,6 +139,7 @@ __device__ __forceinline__ void batch_fast(const BatchPass& bp, long long tile, 
 PG_BT_MX_ALL(F32);
 PG_BT_MX_ALL(FDD);
 PG_BT_MX_ALL(FQ);
+PG_BT_MX_ALL(FX);
 #define PG_BT_DEF_MX(P, N)                                                                                       \
   PG_BT_MX(bt_mx_##P##_##N##_rm) { fast::mixed_tile<fast::P, -1, N, fast::mixed_L<fast::P>(N), true, true, true>(a, tile, sm); }   \
   PG_BT_MX(bt_mx_##P##_##N##_rp) { fast::mixed_tile<fast::P, 1, N, fast::mixed_L<fast::P>(N), true, true, true>(a, tile, sm); }    \
@@ -158,6 +159,8 @@ PG_BT_MX_ALL(FQ);
   case N:                                \
     if (!DOUBLE)                         \
       PG_BT_MX_CALL(F32, N);             \
+    else if (bp.p.quant == 2)            \
+      PG_BT_MX_CALL(FX, N);              \
     else if (bp.p.quant)                 \
       PG_BT_MX_CALL(FQ, N);              \
     else                                 \

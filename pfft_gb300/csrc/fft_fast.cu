@@ -138,8 +138,8 @@ static bool fast_tables(const PassParams& p, int arith, bool pow2, const void** 
   cudaError_t e;
   const bool dct = p.mode == MODE_RE10 || p.mode == MODE_RE01;
   const int fsign = p.mode == MODE_RE10 ? -1 : (p.mode == MODE_RE01 ? 1 : p.sign);
-  if (arith == ARITH_F64) {  // 64-bit fixed point (FX): power-of-two lines
-    *tw = twiddle_table(p.N, fsign < 0 ? TW_FX_FWD_STG : TW_FX_BWD_STG, &e);
+  if (arith == ARITH_F64) {  // 64-bit fixed point (FX): stage-major (radix-8) or natural (mixed radix)
+    *tw = twiddle_table(p.N, pow2 ? (fsign < 0 ? TW_FX_FWD_STG : TW_FX_BWD_STG) : (fsign < 0 ? TW_FX_FWD : TW_FX_BWD), &e);
     if (dct) *tw2 = twiddle_table(p.M, fsign < 0 ? TW_FX_FWD : TW_FX_BWD, &e);
   } else if (arith == ARITH_DF) {
     *tw = twiddle_table(p.N, pow2 ? (fsign < 0 ? TW_DFP_FWD_STG : TW_DFP_BWD_STG) : (fsign < 0 ? TW_DFP_FWD : TW_DFP_BWD),
@@ -163,12 +163,12 @@ bool fast_args(const PassParams& p, int arith, FastArgs* a, bool* row_in, bool* 
   // the mixed-radix kernel reads and writes plain c2c lines only
   if (!pow2 && (!mixed_supported(N) || !plain)) return false;
   if ((p.mode == MODE_RE10 || p.mode == MODE_RE01) && N > 512) return false;
-  // double plans (native FP64 storage and arithmetic class): the radix-8
-  // kernel's 64-bit fixed-point arithmetic on power-of-two c2c, r2c, c2r,
-  // REDFT10 and REDFT01 lines with any window or adjoint weight
-  // (PassParams::quant == 2); every other pass of such a plan runs the
-  // general kernel in FP64
-  if (arith == ARITH_F64 && !(p.quant == 2 && pow2)) return false;
+  // double plans (native FP64 storage and arithmetic class): 64-bit fixed
+  // point (PassParams::quant == 2) on the radix-8 kernel's power-of-two c2c,
+  // r2c, c2r, REDFT10 and REDFT01 lines with any window or adjoint weight,
+  // and on the mixed-radix kernel's plain c2c lines; every other pass of such
+  // a plan runs the general kernel in FP64
+  if (arith == ARITH_F64 && p.quant != 2) return false;
   if (arith != ARITH_F32 && arith != ARITH_DF && arith != ARITH_F64) return false;
   if (p.ashI.en || p.ashO.en) return false;
   if (p.nb > PG_MAX_BATCH) return false;
@@ -264,6 +264,11 @@ int launch_fast_pass(const PassParams& p, int arith, cudaStream_t stream) {
                                           : launch_dct<FDD, 1>(N, a, row_in, row_out, stream));
   if (N & (N - 1)) {  // 3 * 2^a or 5 * 2^a: mixed-radix kernel
     const bool three = N % 3 == 0;
+    if (arith == ARITH_F64)  // 64-bit fixed point
+      return sign < 0 ? (three ? launch_mixed_three<FX, -1>(N, a, row_in, row_out, stream)
+                                 : launch_mixed_five<FX, -1>(N, a, row_in, row_out, stream))
+                        : (three ? launch_mixed_three<FX, 1>(N, a, row_in, row_out, stream)
+                                 : launch_mixed_five<FX, 1>(N, a, row_in, row_out, stream));
     if (arith == ARITH_F32)
       return sign < 0 ? (three ? launch_mixed_three<F32, -1>(N, a, row_in, row_out, stream)
                                  : launch_mixed_five<F32, -1>(N, a, row_in, row_out, stream))

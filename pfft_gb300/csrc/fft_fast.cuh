@@ -503,12 +503,12 @@ __device__ __forceinline__ double fx_to_double(long long Y, int eo) {
 // The tile's entry into FX: v holds the thread's eight values as double bits
 // (gload<FX>); every thread of the block takes part (one barrier).  Returns
 // the exponent of the stored results (fx_to_double) for a length-N line.
-template <int N>
-__device__ __forceinline__ int fx_enter(FX::C (&v)[8], int conj_in) {
+template <int N, int K = 8>
+__device__ __forceinline__ int fx_enter(FX::C (&v)[K], int conj_in) {
   __shared__ unsigned red[32];
   unsigned em = 0;
 #pragma unroll
-  for (int r = 0; r < 8; r++) {
+  for (int r = 0; r < K; r++) {
     em = max(em, (unsigned)(v[r].x >> 32) & 0x7FF00000u);
     em = max(em, (unsigned)(v[r].y >> 32) & 0x7FF00000u);
   }
@@ -521,7 +521,7 @@ __device__ __forceinline__ int fx_enter(FX::C (&v)[8], int conj_in) {
   const int Eraw = (int)(em >> 20);
   const int E = max(Eraw, 1);
 #pragma unroll
-  for (int r = 0; r < 8; r++) {
+  for (int r = 0; r < K; r++) {
     v[r].x = fx_from_bits(v[r].x, E);
     v[r].y = fx_from_bits(v[r].y, E);
     if (conj_in) v[r].y = -v[r].y;
@@ -564,10 +564,11 @@ __device__ __forceinline__ int fx_enter_linked(FX::C (&v)[8], const int (&ex)[8]
 // barrier (each warp's OR of |high words| into slot[warp]), fx_normal_shift
 // after it (the tile's shift: the largest component below 2^60), fx_shift
 // on every value.
-__device__ __forceinline__ unsigned fx_ormag(const FX::C (&v)[8]) {
+template <int K>
+__device__ __forceinline__ unsigned fx_ormag(const FX::C (&v)[K]) {
   unsigned acc = 0;
 #pragma unroll
-  for (int r = 0; r < 8; r++) {
+  for (int r = 0; r < K; r++) {
     const int hx = (int)(v[r].x >> 32), hy = (int)(v[r].y >> 32);
     acc |= (unsigned)(hx ^ (hx >> 31)) | (unsigned)(hy ^ (hy >> 31));
   }

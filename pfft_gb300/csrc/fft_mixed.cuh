@@ -163,9 +163,56 @@ __device__ __forceinline__ void fq_bf5(FDD::C* v) {
   v[3] = fq_sub(m2, n2);
 }
 
+// ---- 64-bit fixed-point butterflies (FX, fft_fast.cuh) ------------------------------
+// The radices' constants c as rounded 64-bit fractions (hi, lo) of c 2^64,
+// or of 1 - c or 1 + c where c itself does not fit below 2^63; a product
+// is then x - x (1 - c) or x (1 + c) - x, each high product rounded once
+// (FX::mh).  x / 2 rounds half to even (no steady bias on the exact ties).
+__device__ __forceinline__ long long fx_half(long long x) { return (x + ((x >> 1) & 1)) >> 1; }
+__device__ __forceinline__ FX::C fx_half(FX::C a) { return {fx_half(a.x), fx_half(a.y)}; }
+__device__ __forceinline__ FX::C fx_kmul(FX::C a, int2 k) { return {FX::mh(a.x, k), FX::mh(a.y, k)}; }
+__device__ __forceinline__ FX::C fx_kmul_1m(FX::C a, int2 k) {  // a (1 - k)
+  return {a.x - FX::mh(a.x, k), a.y - FX::mh(a.y, k)};
+}
+__device__ __forceinline__ FX::C fx_kmul_m1(FX::C a, int2 k) {  // a (k - 1)
+  return {FX::mh(a.x, k) - a.x, FX::mh(a.y, k) - a.y};
+}
+template <int SIGN>
+__device__ __forceinline__ void fx_bf3(FX::C* v) {
+  const int2 k1mS3 = make_int2(575416509, 1033546850);  // (1 - sqrt(3)/2) 2^64
+  const FX::C t = FX::add(v[1], v[2]), u = FX::sub(v[1], v[2]), a0 = v[0];
+  v[0] = FX::add(a0, t);
+  const FX::C m = FX::sub(a0, fx_half(t));
+  const FX::C su = msi<FX, SIGN>(fx_kmul_1m(u, k1mS3));
+  v[1] = FX::add(m, su);
+  v[2] = FX::sub(m, su);
+}
+template <int SIGN>
+__device__ __forceinline__ void fx_bf5(FX::C* v) {
+  const int2 kC1 = make_int2(1327217885, -1079689717);   // cos(2 pi / 5) 2^64
+  const int2 k1pC2 = make_int2(820265763, 1079689717);   // (1 + cos(4 pi / 5)) 2^64
+  const int2 k1mS1 = make_int2(210210662, -581434099);   // (1 - sin(2 pi / 5)) 2^64
+  const int2 k1mS2 = make_int2(1770448860, 1429016722);  // (1 - sin(4 pi / 5)) 2^64
+  const FX::C a0 = v[0];
+  const FX::C t1 = FX::add(v[1], v[4]), t2 = FX::add(v[2], v[3]);
+  const FX::C u1 = FX::sub(v[1], v[4]), u2 = FX::sub(v[2], v[3]);
+  v[0] = FX::add(a0, FX::add(t1, t2));
+  const FX::C m1 = FX::add(a0, FX::add(fx_kmul(t1, kC1), fx_kmul_m1(t2, k1pC2)));
+  const FX::C m2 = FX::add(a0, FX::add(fx_kmul_m1(t1, k1pC2), fx_kmul(t2, kC1)));
+  const FX::C n1 = msi<FX, SIGN>(FX::add(fx_kmul_1m(u1, k1mS1), fx_kmul_1m(u2, k1mS2)));
+  const FX::C n2 = msi<FX, SIGN>(FX::sub(fx_kmul_1m(u1, k1mS2), fx_kmul_1m(u2, k1mS1)));
+  v[1] = FX::add(m1, n1);
+  v[4] = FX::sub(m1, n1);
+  v[2] = FX::add(m2, n2);
+  v[3] = FX::sub(m2, n2);
+}
+
 template <class P, int SIGN, int R>
 __device__ __forceinline__ void bfR(typename P::C* v) {
-  if constexpr (std::is_same<P, FQ>::value) {
+  if constexpr (is_fx<P>() && (R == 3 || R == 5)) {
+    if constexpr (R == 3) fx_bf3<SIGN>(v);
+    if constexpr (R == 5) fx_bf5<SIGN>(v);
+  } else if constexpr (std::is_same<P, FQ>::value) {
     if constexpr (R == 2 || R == 4) {
       float2 c1, c2;
       fq_grid<R>(v, c1, c2);
@@ -211,7 +258,8 @@ struct MixedStage {
     return p;
   }
 
-  // twiddles and butterflies of this stage (inputs in v, outputs in place)
+  // twiddles and butterflies of this stage (inputs in v, outputs in place;
+  // FX twiddles carry 1/4, element 0 of a twiddled stage takes it alone)
   static __device__ __forceinline__ void compute(C* v, int t, const void* tw) {
     constexpr int Ns = ns();
 #pragma unroll
@@ -220,6 +268,7 @@ struct MixedStage {
       if (Ns > 1) {
         const int k = b % Ns;
         constexpr int step = N / (Ns * R);
+        if constexpr (is_fx<P>()) v[i * R] = P::tw0(v[i * R]);
 #pragma unroll
         for (int r = 1; r < R; r++) v[i * R + r] = P::mul(v[i * R + r], P::template twd<SIGN>(P::ldw(tw, k * r * step, N)));
       }
@@ -236,13 +285,17 @@ struct MixedStage {
   }
 };
 
+// fxsh (FX): the shifts and twiddle scalings so far, added to the results'
+// exponent; each exchange brings the tile's largest component to 59 bits
+// (every thread of the block takes part: the exchanges are block-wide)
 template <class P, int SIGN, int N, int E, int s>
-__device__ __forceinline__ void mixed_stages(typename P::C* v, int t, const void* tw, typename P::S* line) {
+__device__ __forceinline__ void mixed_stages(typename P::C (&v)[E], int t, const void* tw, typename P::S* line, int& fxsh) {
   typedef MixedStage<P, SIGN, N, E, s> St;
   St::compute(v, t, tw);
   if constexpr (s + 1 < St::NS) {
     // exchange: outputs to shared memory, next stage's inputs back
     __syncthreads();  // the previous exchange's loads are done
+    if constexpr (is_fx<P>()) fx_ormag_publish(fx_ormag(v), fx_slots() + 32 * (s & 1));
 #pragma unroll
     for (int i = 0; i < E / St::R; i++)
 #pragma unroll
@@ -253,7 +306,13 @@ __device__ __forceinline__ void mixed_stages(typename P::C* v, int t, const void
     for (int i = 0; i < E / R2; i++)
 #pragma unroll
       for (int r = 0; r < R2; r++) v[i * R2 + r] = P::lds(line[pad<P>(t + i * (N / E) + r * (N / R2))]);
-    mixed_stages<P, SIGN, N, E, s + 1>(v, t, tw, line);
+    if constexpr (is_fx<P>()) {
+      const int sh = fx_normal_shift(fx_slots() + 32 * (s & 1));
+#pragma unroll
+      for (int q = 0; q < E; q++) v[q] = {fx_shift(v[q].x, sh), fx_shift(v[q].y, sh)};
+      fxsh += sh + 2;  // the next stage is twiddled
+    }
+    mixed_stages<P, SIGN, N, E, s + 1>(v, t, tw, line, fxsh);
   }
 }
 
@@ -306,10 +365,18 @@ __device__ __forceinline__ void mixed_tile(const FastArgs& a, long long blk, uns
       for (int r = 0; r < R0; r++) {
         const long long e = t + i * TPL + r * (N / R0);
         C x = gload<P, CG>(src + e * a.sIa, a.in_df);
-        v[i * R0 + r] = a.conj_in ? P::conj(x) : x;
+        if constexpr (is_fx<P>())
+          v[i * R0 + r] = x;  // double bits; fx_enter conjugates
+        else
+          v[i * R0 + r] = a.conj_in ? P::conj(x) : x;
       }
   }
-  mixed_stages<P, SIGN, N, E, 0>(v, t, tw, line);
+  // FX: the tile onto its grid; sdf the results' exponent
+  int fxsh = 0, sdf = a.out_df;
+  int fx_e = 0;
+  if constexpr (is_fx<P>()) fx_e = fx_enter<N, E>(v, a.conj_in);
+  mixed_stages<P, SIGN, N, E, 0>(v, t, tw, line, fxsh);
+  if constexpr (is_fx<P>()) sdf = fx_e == INT_MIN ? INT_MIN : fx_e + fxsh;
   // last stage: output r of butterfly i is element t + i * TPL + r * N/RL
   if (ROW_IN == ROW_OUT) {
     if (live) {
@@ -320,7 +387,7 @@ __device__ __forceinline__ void mixed_tile(const FastArgs& a, long long blk, uns
         for (int r = 0; r < RL; r++) {
           const int e = t + i * TPL + r * (N / RL);
           C o = v[i * RL + r];
-          gstore<P>(dst + (long long)e * a.sOa, a.conj_out ? P::conj(o) : o, a.out_df);
+          gstore<P>(dst + (long long)e * a.sOa, a.conj_out ? P::conj(o) : o, sdf);
         }
     }
     return;
@@ -341,7 +408,7 @@ __device__ __forceinline__ void mixed_tile(const FastArgs& a, long long blk, uns
     for (int q = 0; q < E; q++) {
       const int k = t2 + q * TPL;
       C o = P::lds(line2[pad<P>(k)]);
-      gstore<P>(d2 + (long long)k * a.sOa, a.conj_out ? P::conj(o) : o, a.out_df);
+      gstore<P>(d2 + (long long)k * a.sOa, a.conj_out ? P::conj(o) : o, sdf);
     }
   }
 }

@@ -140,6 +140,7 @@ static bool link_fx(Plan* pl, PassProgram* prog, std::vector<int*>* lexp) {
     PassParams& b = prog->passes[i + 1].p;
     const bool b_plain = b.mode == MODE_C2C && b.Zi == 0 && b.Ni == b.N && b.Zo == 0 && b.No == b.N && !b.wmode;
     if (!b_plain || (a.mode != MODE_C2C && a.mode != MODE_R2C)) continue;
+    if ((a.N & (a.N - 1)) || (b.N & (b.N - 1))) continue;  // the radix-8 kernel on both sides
     if (!fast_pass_eligible(a, pl->arith) || !fast_pass_eligible(b, pl->arith)) continue;
     // b's input dimensions onto a's output dimensions.  Both passes' planner
     // merged dimensions contiguous on both of their sides, so one of b's

@@ -8,10 +8,14 @@ C2  256^3 r2c / c2r, float64 and float32, N(0,1) real input, PADDED_R2C
     definitions: the oracle evaluates r2r lines directly, O(n^2) per line, and
     is checked against scipy at smaller sizes).
 C5  512^3 complex128 and 1024^3 complex64 forward + backward (size-independent
-    properties: round trip and Parseval), 64^4 complex128 against the oracle.
+    properties: round trip and Parseval), 512^3 complex128 (forward and
+    backward, three double arithmetics), 1024 x 1024 x 256 complex64 and
+    64^4 complex128 against the oracle.
 
 Inputs are seeded synthetic data with the suite's distributions.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -110,6 +114,37 @@ def test_c5_512cube_complex128_roundtrip_block_quantised(cuda, pfft_lib):
     with double_arith("double-dfq"):
         rt, pv = _roundtrip_large(cuda, (512, 512, 512), "double")
     assert rt <= 1e-12 and pv <= 1e-12, (rt, pv)
+
+
+@pytest.mark.parametrize("sign", [-1, 1])
+@pytest.mark.parametrize("prec,tol", [("double", 1e-15), ("double-f64", 1e-15), ("double-dfq", 1e-12)])
+def test_c5_512cube_complex128_against_oracle(cuda, pfft_lib, sign, prec, tol):
+    """The headline size element for element against the FP64 oracle, forward
+    and backward, in the default arithmetic (64-bit fixed point), native FP64
+    and the opt-in block-quantised float-float."""
+    n = (512, 512, 512)
+    req = Req("c2c", n, sign=sign)
+    x = np.random.default_rng(8 + sign).uniform(-1, 1, 2 * 512 ** 3)
+    ref = oracle_run(req, x, nthreads=os.cpu_count())
+    y = gpu_run(req, x, prec=prec)
+    e = rel_l2(y, ref)
+    del y, ref
+    cuda.cuda.empty_cache()
+    assert e <= tol, e
+
+
+def test_c5_1024x1024x256_complex64_against_oracle(cuda, pfft_lib):
+    """complex64 at a 2^28-point size against the FP64 oracle (the float
+    API's input is the oracle's input rounded to float)."""
+    n = (1024, 1024, 256)
+    req = Req("c2c", n)
+    x = np.random.default_rng(12).uniform(-1, 1, 2 * int(np.prod(n))).astype(np.float32).astype(np.float64)
+    ref = oracle_run(req, x, nthreads=os.cpu_count())
+    y = gpu_run(req, x, prec="float")
+    e = rel_l2(y, ref)
+    del y, ref
+    cuda.cuda.empty_cache()
+    assert e <= 1e-6, e
 
 
 def test_c5_1024cube_complex64_roundtrip(cuda, pfft_lib):

@@ -37,6 +37,27 @@ def test_fx_no_less_accurate_than_native_fp64(cuda, pfft_lib, n, flags, sign):
     assert e_fx <= 1.25 * e_nat + 1e-17, (e_fx, e_nat)
 
 
+MIXED_SHAPES = [(24, 40, 48), (96, 96, 8), (2, 768, 4), (640, 4, 2), (160, 2, 320), (80, 384, 1), (192, 6, 10)]
+
+
+@pytest.mark.parametrize("sign", [-1, 1])
+@pytest.mark.parametrize("flags", [0, pg.PFFT_TRANSPOSED_OUT])
+@pytest.mark.parametrize("n", MIXED_SHAPES)
+def test_fx_mixed_radix_no_less_accurate_than_native_fp64(cuda, pfft_lib, n, flags, sign):
+    """3 * 2^a and 5 * 2^a lengths run FX on the mixed-radix kernel (radix-3
+    and radix-5 butterflies with 64-bit fixed-point constants): the same bar
+    as the radix-8 kernel against the oracle and native FP64."""
+    req = Req("c2c", n, sign=sign, flags=flags)
+    rng = np.random.default_rng(sum(n) * 7 + sign + flags)
+    x = random_input(req, rng)
+    ref = oracle_run(req, x)
+    fx = gpu_run(req, x, prec="double")
+    nat = gpu_run(req, x, prec="double-f64")
+    e_fx, e_nat = rel_l2(fx, ref), rel_l2(nat, ref)
+    assert e_fx <= 1e-15, e_fx
+    assert e_fx <= 1.25 * e_nat + 1e-17, (e_fx, e_nat)
+
+
 def _exact_dft3(x, n, sign=-1):
     """3-D DFT in extended precision (numpy longdouble: 64- or 113-bit
     mantissa), one axis at a time by explicit DFT matrices: a reference more
@@ -65,12 +86,13 @@ def _rel(got, exact):
 
 
 @pytest.mark.parametrize("dist", ["uniform", "spread", "spike", "spike_alone", "one_line"])
-def test_fx_dynamic_range_against_extended_precision(cuda, pfft_lib, dist):
+@pytest.mark.parametrize("n", [(8, 16, 32), (24, 40, 8)])
+def test_fx_dynamic_range_against_extended_precision(cuda, pfft_lib, dist, n):
     """Uniform values, values spread over 2^+-40, a single large value among
     small ones (and alone), one line a million times larger than the rest:
     FX's error against an extended-precision DFT stays within 1.25x native
-    FP64's error, or within one double rounding (2^-53) of the result."""
-    n = (8, 16, 32)
+    FP64's error, or within one double rounding (2^-53) of the result, on
+    the radix-8 kernel and on the mixed-radix one (24 = 3 * 8, 40 = 5 * 8)."""
     req = Req("c2c", n)
     rng = np.random.default_rng(3)
     x = random_input(req, rng)
