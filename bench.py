@@ -794,8 +794,8 @@ def main():
         "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": {0: "f32",
-                  1: ("f64 storage, int64 block-fixed-point arithmetic on the radix-8 passes (58 bits against the "
-                      "tile maximum; measured no less accurate than native FP64), FP64 elsewhere")
+                  1: ("f64 storage, int64 block-fixed-point arithmetic on the radix-8 and mixed-radix passes (58-60 "
+                      "bits against the tile maximum; measured no less accurate than native FP64), FP64 elsewhere")
                   if dmode == 2 else "f64 (native FP64 arithmetic)",
                   2: "f64 storage, float-float arithmetic" +
                   (" (block-quantised radix-8 stages)" if dmode == 3 else " (TwoSum)")}[plan_arith],

@@ -111,8 +111,15 @@ struct GcMove {
   int* err;
   unsigned epoch;
   unsigned rs_magic;     // 0xFFFFFFFF / RS + 1 (RS > 1): f / RS = umulhi(f, rs_magic) for f, RS < 2^16
+  unsigned rsv_magic;    // the same for RSV = RS / W, the 16-byte vectors of a block row (vector path)
   long long spin_limit;
 };
+
+// Vector path of the move: every row start, row length and the buffer 16-byte
+// aligned; each thread then moves its share of a chunk (GC_STAGE_BYTES / 16 /
+// GC_THREADS = 8 vectors) as 16-byte vectors, four loads issued before their
+// stores, instead of one 8-byte access at a time.
+constexpr int GC_VPT = GC_STAGE_BYTES / 16 / GC_THREADS;
 
 __device__ __forceinline__ long long gc_box_start(const GcMove& m, long long row) {
   const long long j0 = row / m.n1, j1 = row - j0 * m.n1;
@@ -121,8 +128,51 @@ __device__ __forceinline__ long long gc_box_start(const GcMove& m, long long row
 
 // EXPAND: block rows -> interior box rows, chunks from the back; otherwise
 // interior box rows -> block rows, chunks from the front
-template <class T, bool EXPAND>
-__global__ void __launch_bounds__(GC_THREADS) k_gc_move(T* __restrict__ data, const GcMove m) {
+// chunk's rows <-> stage as 16-byte vectors (VEC path): contiguous block
+// rows on one side, box rows (start boxrow[q], RSV vectors) on the other;
+// four vectors in flight per thread, twice
+template <class T, bool TO_STAGE, bool BOX>
+__device__ __forceinline__ void gc_vec_move(T* __restrict__ data, uint4* stv, const long long* boxrow, long long blk0,
+                                            unsigned nv, const GcMove& m) {
+  constexpr int W = 16 / (int)sizeof(T);
+  constexpr int K = 4;
+  const unsigned RSV = (unsigned)(m.RS / W);
+#pragma unroll 1
+  for (int k0 = 0; k0 < GC_VPT; k0 += K) {
+    uint4 tmp[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      const unsigned f = threadIdx.x + (k0 + k) * GC_THREADS;
+      if (f >= nv) continue;
+      if (TO_STAGE) {
+        if (BOX) {
+          const unsigned q = RSV == 1 ? f : __umulhi(f, m.rsv_magic);
+          tmp[k] = ((const uint4*)data)[boxrow[q] / W + (f - q * RSV)];
+        } else {
+          tmp[k] = ((const uint4*)data)[blk0 / W + f];
+        }
+      } else {
+        tmp[k] = stv[f];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      const unsigned f = threadIdx.x + (k0 + k) * GC_THREADS;
+      if (f >= nv) continue;
+      if (TO_STAGE) {
+        stv[f] = tmp[k];
+      } else if (BOX) {
+        const unsigned q = RSV == 1 ? f : __umulhi(f, m.rsv_magic);
+        ((uint4*)data)[boxrow[q] / W + (f - q * RSV)] = tmp[k];
+      } else {
+        ((uint4*)data)[blk0 / W + f] = tmp[k];
+      }
+    }
+  }
+}
+
+template <class T, bool EXPAND, bool VEC>
+__global__ void __launch_bounds__(GC_THREADS, VEC ? 4 : 1) k_gc_move(T* __restrict__ data, const GcMove m) {
   __shared__ __align__(16) unsigned char stage_raw[GC_STAGE_BYTES];
   __shared__ long long boxrow[GC_MAX_ROWS];
   __shared__ long long s_chunk;
@@ -146,7 +196,9 @@ __global__ void __launch_bounds__(GC_THREADS) k_gc_move(T* __restrict__ data, co
     __syncthreads();
     const unsigned nsc = (unsigned)(nr * m.RS);
     // read the chunk's rows
-    if (EXPAND) {
+    if (VEC) {
+      gc_vec_move<T, true, !EXPAND>(data, (uint4*)stage_raw, boxrow, r_lo * m.RS, nsc / (16 / sizeof(T)), m);
+    } else if (EXPAND) {
       const T* src = data + r_lo * m.RS;  // block rows are contiguous
       for (unsigned f = tid; f < nsc; f += GC_THREADS) stage[f] = src[f];
     } else {
@@ -194,7 +246,9 @@ __global__ void __launch_bounds__(GC_THREADS) k_gc_move(T* __restrict__ data, co
     __threadfence();
     __syncthreads();
     // write
-    if (EXPAND) {
+    if (VEC) {
+      gc_vec_move<T, false, EXPAND>(data, (uint4*)stage_raw, boxrow, r_lo * m.RS, nsc / (16 / sizeof(T)), m);
+    } else if (EXPAND) {
       for (unsigned f = tid; f < nsc; f += GC_THREADS) {
         const unsigned q = m.RS == 1 ? f : __umulhi(f, m.rs_magic);
         data[boxrow[q] + (f - q * (unsigned)m.RS)] = stage[f];
@@ -495,6 +549,8 @@ GcMove gc_move_args(GcPlan* p) {
   if (++p->epoch == 0) p->epoch = 1;  // flags start at 0, so epoch 0 is never used
   m.epoch = p->epoch;
   m.rs_magic = m.RS > 1 ? (unsigned)(0xFFFFFFFFull / (unsigned long long)m.RS + 1) : 0u;
+  const long long W = 16 / esz(p), RSV = m.RS / W;
+  m.rsv_magic = RSV > 1 ? (unsigned)(0xFFFFFFFFull / (unsigned long long)RSV + 1) : 0u;
   m.spin_limit = 20000000;  // about 2 s of 64 ns naps
   return m;
 }
@@ -505,7 +561,11 @@ int gc_move(GcPlan* p, void* data) {
   if (e != cudaSuccess) return (int)e;
   const GcMove m = gc_move_args(p);
   const long long grid = std::min<long long>(m.nchunks, (long long)p->sms * 4);
-  if (grid > 0) k_gc_move<T, EXPAND><<<(unsigned)grid, GC_THREADS, 0, p->stream>>>((T*)data, m);
+  // 16-byte vectors when every row start and length is a multiple of 16 bytes
+  const long long W = 16 / (long long)sizeof(T);
+  const bool vec = ((uintptr_t)data & 15) == 0 && m.RS % W == 0 && m.RB % W == 0 && m.off2 % W == 0;
+  if (grid > 0 && vec) k_gc_move<T, EXPAND, true><<<(unsigned)grid, GC_THREADS, 0, p->stream>>>((T*)data, m);
+  if (grid > 0 && !vec) k_gc_move<T, EXPAND, false><<<(unsigned)grid, GC_THREADS, 0, p->stream>>>((T*)data, m);
   e = cudaGetLastError();
   if (e != cudaSuccess) return (int)e;
   return (int)cudaMemcpyAsync(p->h_err, p->ctl + 1, sizeof(int), cudaMemcpyDeviceToHost, p->stream);

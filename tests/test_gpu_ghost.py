@@ -70,6 +70,10 @@ def run_gc(torch, kind, n, gcb, gca, prec="double", flags=0, howmany=1, reduce=F
     ("c", [40, 64, 33], [0, 0, 0], [0, 0, 3], 0),
     ("r", [50, 40, 1], [2, 3, 0], [1, 0, 0], 0),
     ("c", [4, 3, 2100], [1, 1, 1], [1, 1, 1], 0),
+    # 16-byte vector moves (every row start and length a multiple of 16 bytes)
+    # with many chunks, in both precisions, and a real block on that path
+    ("c", [48, 40, 64], [0, 1, 2], [2, 0, 2], 0),
+    ("r", [16, 12, 8], [2, 0, 2], [2, 4, 2], 0),
 ])
 def test_exchange_bit_exact(cuda, pfft_lib, prec, kind, n, gcb, gca, flags):
     if flags & pg.PFFT_GC_TRANSPOSED:
@@ -88,7 +92,8 @@ def test_exchange_bit_exact(cuda, pfft_lib, prec, kind, n, gcb, gca, flags):
 def test_reduce(cuda, pfft_lib, prec, tol):
     for kind, n, gcb, gca in [("c", [8, 8, 8], [0, 0, 0], [4, 0, 0]), ("c", [5, 6, 7], [7, 1, 0], [0, 9, 2]),
                               ("r", [64, 48, 40], [3, 0, 1], [0, 2, 5]), ("c", [40, 64, 33], [0, 0, 0], [0, 0, 3]),
-                              ("r", [50, 40, 1], [2, 3, 0], [1, 0, 0]), ("c", [4, 3, 2100], [1, 1, 1], [1, 1, 1])]:
+                              ("r", [50, 40, 1], [2, 3, 0], [1, 0, 0]), ("c", [4, 3, 2100], [1, 1, 1], [1, 1, 1]),
+                              ("c", [48, 40, 64], [0, 1, 2], [2, 0, 2])]:
         got, ref = run_gc(cuda, kind, n, gcb, gca, prec, reduce=True)
         err = np.linalg.norm(got - ref) / np.linalg.norm(ref)
         assert err < tol, (n, err)
