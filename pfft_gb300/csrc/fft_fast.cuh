@@ -381,6 +381,20 @@ __device__ __forceinline__ void bf8x(typename P::C* v) {
 // arithmetic.  Results are rounded to nearest double when stored
 // (x = Y * 2^(E - 1080 + the stages' shifts)).  A tile holding an infinity
 // or NaN stores NaN everywhere; results below 2^-1022 are stored as zero.
+// 32x32 -> 64-bit signed products, alone or added to a 64-bit value, as one
+// mul.wide / mad.wide each, so that a chain of them accumulates in the
+// multiplier's own 64-bit adder
+__device__ __forceinline__ long long fx_mulw(int a, int b) {
+  long long d;
+  asm("mul.wide.s32 %0, %1, %2;" : "=l"(d) : "r"(a), "r"(b));
+  return d;
+}
+__device__ __forceinline__ long long fx_madw(int a, int b, long long c) {
+  long long d;
+  asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(c));
+  return d;
+}
+
 struct FX {
   typedef longlong2 S;  // shared memory: (re, im)
   typedef double2 G;
@@ -416,9 +430,9 @@ struct FX {
     const unsigned xu = (unsigned)x;
     const int xl = (int)xu;
     const int xh = (int)(x >> 32) + (int)(xu >> 31);
-    const long long s = (long long)xh * w.y + (long long)xl * w.x;
+    const long long s = fx_madw(xl, w.x, fx_mulw(xh, w.y));
     const int c = (int)(s >> 32) + (int)((unsigned)s >> 31);
-    return (long long)xh * w.x + (long long)c;
+    return fx_madw(xh, w.x, (long long)c);
   }
   // (x + i y) (c + i s) / 2^64, each part rounded once: with x = xh 2^32 +
   // xl and y, c, s split alike, Re = xh ch - yh sh + round(m / 2^32), m = xh
@@ -430,12 +444,11 @@ struct FX {
     const unsigned xu = (unsigned)a.x, yu = (unsigned)a.y;
     const int xl = (int)xu, yl = (int)yu;
     const int xh = (int)(a.x >> 32) + (int)(xu >> 31), yh = (int)(a.y >> 32) + (int)(yu >> 31);
-    const long long rm = (long long)xh * w.a.y + (long long)xl * w.a.x + (long long)yh * w.n.y + (long long)yl * w.n.x;
-    const long long im = (long long)xh * w.a.w + (long long)xl * w.a.z + (long long)yh * w.a.y + (long long)yl * w.a.x;
+    const long long rm = fx_madw(yl, w.n.x, fx_madw(yh, w.n.y, fx_madw(xl, w.a.x, fx_mulw(xh, w.a.y))));
+    const long long im = fx_madw(yl, w.a.x, fx_madw(yh, w.a.y, fx_madw(xl, w.a.z, fx_mulw(xh, w.a.w))));
     const int rc = (int)(rm >> 32) + (int)((unsigned)rm >> 31);
     const int ic = (int)(im >> 32) + (int)((unsigned)im >> 31);
-    return {(long long)xh * w.a.x + (long long)yh * w.n.x + (long long)rc,
-            (long long)xh * w.a.z + (long long)yh * w.a.x + (long long)ic};
+    return {fx_madw(xh, w.a.x, fx_madw(yh, w.n.x, (long long)rc)), fx_madw(xh, w.a.z, fx_madw(yh, w.a.x, (long long)ic))};
   }
   static __device__ __forceinline__ K8 c8() { return {}; }
   // a * sqrt(1/2) = a - a (1 - sqrt(1/2)), the product rounded
@@ -589,21 +602,21 @@ __device__ __forceinline__ int fx_normal_shift(const unsigned* slot, int bits = 
   const int bl = 32 + (m ? 32 - __clz((int)m) : 0);
   return bl - (bits - 1);
 }
-// x * 2^-s for -31 < s < 32, rounded to nearest (the same s in every thread:
-// no divergence)
-__device__ __forceinline__ long long fx_shift(long long x, int s) {
-  if (s > 0) x += 1ll << (s - 1);
-  unsigned lo = (unsigned)x;
-  int hi = (int)(x >> 32);
-  if (s >= 0) {
-    lo = __funnelshift_r(lo, (unsigned)hi, s);
-    hi = hi >> s;
-  } else {
-    const int t = -s;
-    hi = (int)__funnelshift_l(lo, (unsigned)hi, t);
-    lo = lo << t;
+// v * 2^-s for every value, -31 < s < 32, rounded to nearest (ties up) for
+// s > 0, exact for s <= 0 (no value loses a bit: the tile's largest is below
+// 2^32 when s < 0).  s is the same in every thread of the block: one
+// uniform branch picks the direction, and each value costs a 64-bit add and
+// shift or a shift alone.
+template <int K>
+__device__ __forceinline__ void fx_shift_all(FX::C (&v)[K], int s) {
+  if (s > 0) {
+    const long long h = 1ll << (s - 1);
+#pragma unroll
+    for (int r = 0; r < K; r++) v[r] = {(v[r].x + h) >> s, (v[r].y + h) >> s};
+  } else if (s < 0) {
+#pragma unroll
+    for (int r = 0; r < K; r++) v[r] = {v[r].x << -s, v[r].y << -s};
   }
-  return (long long)(((unsigned long long)(unsigned)hi << 32) | lo);
 }
 __device__ __forceinline__ unsigned* fx_slots() {
   __shared__ unsigned slots[2][32];  // per-warp ORs of two consecutive stages
@@ -624,8 +637,7 @@ __device__ __forceinline__ int fx_store_normalise(FX::C (&v)[K], unsigned* slot)
   fx_ormag_publish(acc, slot);
   __syncthreads();
   const int sh = fx_normal_shift(slot, 58);
-#pragma unroll
-  for (int r = 0; r < K; r++) v[r] = {fx_shift(v[r].x, sh), fx_shift(v[r].y, sh)};
+  fx_shift_all(v, sh);
   return sh;
 }
 
@@ -1052,8 +1064,7 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
     for (int r = 0; r < 8; r++) v[r] = P::lds(line[pad<P>(t + r * TPL)]);
     if constexpr (is_fx<P>()) {
       const int sh = fx_normal_shift(fx_slots() + 32 * (s & 1));
-#pragma unroll
-      for (int r = 0; r < 8; r++) v[r] = {fx_shift(v[r].x, sh), fx_shift(v[r].y, sh)};
+      fx_shift_all(v, sh);
       fx_sh += sh + 2;
     }
     const int k = t % Ns;
@@ -1107,14 +1118,17 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
     }
     C w[8];
 #pragma unroll
+    for (int b = 0; b < NB; b++)
+#pragma unroll
+      for (int r = 0; r < Q; r++) w[b * Q + r] = P::lds(line[pad<P>(t + b * TPL + r * NQ)]);
+    if constexpr (is_fx<P>()) fx_shift_all(w, qsh);
+#pragma unroll
     for (int b = 0; b < NB; b++) {
       const int j = t + b * TPL;
 #pragma unroll
       for (int r = 0; r < Q; r++) {
-        C x = P::lds(line[pad<P>(j + r * NQ)]);
-        if constexpr (is_fx<P>()) x = {fx_shift(x.x, qsh), fx_shift(x.y, qsh)};
-        x = r > 0 ? P::mul(x, P::template twd<SIGN>(P::ldw(tw, NQ - 8 + (r - 1) * NQ + j, TWN))) : P::tw0(x);
-        w[b * Q + r] = x;
+        const C x = w[b * Q + r];
+        w[b * Q + r] = r > 0 ? P::mul(x, P::template twd<SIGN>(P::ldw(tw, NQ - 8 + (r - 1) * NQ + j, TWN))) : P::tw0(x);
       }
       if (Q == 2) {
         C x0 = w[b * 2], x1 = w[b * 2 + 1];

@@ -308,8 +308,7 @@ __device__ __forceinline__ void mixed_stages(typename P::C (&v)[E], int t, const
       for (int r = 0; r < R2; r++) v[i * R2 + r] = P::lds(line[pad<P>(t + i * (N / E) + r * (N / R2))]);
     if constexpr (is_fx<P>()) {
       const int sh = fx_normal_shift(fx_slots() + 32 * (s & 1));
-#pragma unroll
-      for (int q = 0; q < E; q++) v[q] = {fx_shift(v[q].x, sh), fx_shift(v[q].y, sh)};
+      fx_shift_all(v, sh);
       fxsh += sh + 2;  // the next stage is twiddled
     }
     mixed_stages<P, SIGN, N, E, s + 1>(v, t, tw, line, fxsh);
