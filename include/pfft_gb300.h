@@ -65,7 +65,8 @@ int pfft_gb300_pass_kernel(const pfft_plan plan, int i);
 int pfftf_gb300_pass_kernel(const pfftf_plan plan, int i);
 /* Fixed-point mantissas kept across pass i's boundaries (double plans, mode
  * 2): bit 0 = its input holds the previous pass's mantissas, bit 1 = its
- * output keeps them for the next pass; -1 = no such pass. */
+ * output keeps them for the next pass; bit 2 = the pass (r2c or REDFT10)
+ * transforms two real lines per complex line; -1 = no such pass. */
 int pfft_gb300_pass_fx_link(const pfft_plan plan, int i);
 int pfftf_gb300_pass_fx_link(const pfftf_plan plan, int i);
 /* Arithmetic a plan runs in: 0 FP32 (float API), 1 FP64 class (modes 1 and 2

@@ -379,7 +379,7 @@ void do_execute(Plan* pl, void* in, void* out) {
   int PX##gb300_pass_fx_link(const PX##plan plan, int i) {                                              \
     if (!plan || i < 0 || i >= (int)plan->p->fwd.passes.size()) return -1;                                \
     const PassParams& q = plan->p->fwd.passes[i].p;                                                       \
-    return (q.fx_in ? 1 : 0) | (q.fx_out ? 2 : 0);                                                        \
+    return (q.fx_in ? 1 : 0) | (q.fx_out ? 2 : 0) | (q.pair ? 4 : 0);                                     \
   }                                                                                                       \
   int PX##gb300_plan_arith(const PX##plan plan) {                                                        \
     if (!plan) return -1;                                                                                 \

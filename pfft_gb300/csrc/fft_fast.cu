@@ -208,6 +208,18 @@ bool fast_args(const PassParams& p, int arith, FastArgs* a, bool* row_in, bool* 
   }
   a->gin_k = p.gin_k;
   a->gout_off = p.gout_off;
+  // paired real lines: batch dimension 0 halved, its odd lines the partners
+  a->pair = 0;
+  if (p.pair && arith == ARITH_F64 && !p.fx_in && !p.fx_out && p.nb >= 1 && p.bext[0] % 2 == 0 &&
+      (p.mode == MODE_R2C || p.mode == MODE_RE10)) {
+    a->pair = 1;
+    a->pairI = p.bsI[0];
+    a->pairO = p.bsO[0];
+    a->bext[0] = p.bext[0] / 2;
+    a->bsI[0] = 2 * p.bsI[0];
+    a->bsO[0] = 2 * p.bsO[0];
+    a->nlines = p.nlines / 2;
+  }
   a->Zi = p.Zi;
   a->Ni = p.Ni;
   a->Zo = p.Zo;

@@ -714,6 +714,11 @@ struct FastArgs {
   long long gin_pext[2 * PG_MAX_BATCH], gin_pcoef[2 * PG_MAX_BATCH];
   long long gin_bofs[PG_MAX_BATCH];
   long long gin_k, gout_off;
+  // paired real lines (PassParams::pair): each line of the tile is real
+  // line a (at the line's offsets) and real line b (at + pairI on the input
+  // side, + pairO on the output side)
+  int pair;
+  long long pairI, pairO;
 };
 
 // global element access: native format, or float-float pairs for the
@@ -867,6 +872,12 @@ __device__ __forceinline__ typename P::C rx(const FastArgs& a, long long off, in
 template <class P, bool CG, bool DCT = false>
 __device__ __forceinline__ typename P::C load_elem(const FastArgs& a, long long off, int e, int N) {
   typedef typename P::C C;
+  if constexpr (is_fx<P>()) {
+    if (a.pair && (a.mode == 1 || a.mode == 3)) {  // r2c / REDFT10: line a's input as the real part, line b's as the imaginary
+      const int j = DCT ? (2 * e < N ? 2 * e : 2 * (N - 1 - e) + 1) : e;
+      return {rx<P, CG>(a, off, j).x, rx<P, CG>(a, off + a.pairI, j).x};
+    }
+  }
   if constexpr (DCT) {
     if (a.mode == 3) return rx<P, CG>(a, off, 2 * e < N ? 2 * e : 2 * (N - 1 - e) + 1);
     C xk = rx<P, CG>(a, off, e);
@@ -922,6 +933,41 @@ __device__ __forceinline__ void store_elem(const FastArgs& a, long long off, int
     rstore<P>(a.dst, off + (long long)k * a.sOa, v, eo);
   else
     gput<P>(a, (typename P::G*)a.dst + off + (long long)k * a.sOa, v, is_fx<P>() ? eo : a.out_df);
+}
+
+// Paired real lines (FastArgs::pair): the thread's outputs z[pos[r]] of the
+// complex line z = x_a + i x_b (line `l` of the tile) go through shared
+// memory; then, with the output side's thread mapping (rows: a line's
+// threads along it; columns: consecutive threads on consecutive lines, so
+// that both real lines' stores stay coalesced), each thread takes z[k] and
+// z[N - k] of eight positions k: X_a[k] = (z[k] + conj z[N - k]) / 2 and
+// X_b[k] = -i (z[k] - conj z[N - k]) / 2, each halving rounded half to even
+// (the sums stay below 2^62.5, the halves below 2^61.5, so that a REDFT10
+// rotation of them cannot overflow), stored as two lines.  Every thread of
+// the block takes part (two barriers).
+template <class P, bool DCT, bool ROW_OUT, int N, int L, int LSP, int K>
+__device__ __forceinline__ void fx_pair_store(const FastArgs& a, const typename P::C (&v)[K], const int (&pos)[K], int l,
+                                              typename P::S* buf, const long long* offO, long long g0, int eo) {
+  typedef typename P::C C;
+  constexpr int TPL = N / 8;
+  __syncthreads();  // the last exchange's loads are done
+#pragma unroll
+  for (int r = 0; r < K; r++) buf[l * LSP + pad<P>(pos[r])] = P::sts(v[r]);
+  __syncthreads();
+  const int l2 = ROW_OUT ? (int)threadIdx.x / TPL : (int)threadIdx.x % L;
+  const int t2 = ROW_OUT ? (int)threadIdx.x % TPL : (int)threadIdx.x / L;
+  if (g0 + l2 >= a.nlines) return;
+  const typename P::S* line = buf + l2 * LSP;
+  const auto half = [](long long x) { return (x + ((x >> 1) & 1)) >> 1; };
+#pragma unroll
+  for (int r = 0; r < 8; r++) {
+    const int k = t2 + r * TPL;
+    const C z = P::lds(line[pad<P>(k)]), zm = P::lds(line[pad<P>((N - k) & (N - 1))]);
+    const C xa = {half(z.x + zm.x), half(z.y - zm.y)};
+    const C xb = {half(z.y + zm.y), half(zm.x - z.x)};
+    store_elem<P, DCT>(a, offO[l2], k, xa, N, eo);
+    store_elem<P, DCT>(a, offO[l2] + a.pairO, k, xb, N, eo);
+  }
 }
 
 // bytes before the exchange area of a tile: the lines' input and output
@@ -1080,6 +1126,15 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
   }
   if (Q == 1) {
     // v holds the last stage (Ns = N/8, k = t): outputs y[t + r*TPL]
+    if constexpr (IO != 0 && is_fx<P>()) {
+      if (a.pair && (a.mode == 1 || a.mode == 3)) {  // r2c / REDFT10: separate the two spectra
+        int pos[8];
+#pragma unroll
+        for (int r = 0; r < 8; r++) pos[r] = t + r * TPL;
+        fx_pair_store<P, IO == 2, ROW_OUT, N, L, LSP>(a, v, pos, l, buf, offO, g0, sdf);
+        return;
+      }
+    }
     if (ROW_IN == ROW_OUT) {
       if (live) {
         if constexpr (IO == 0) {
@@ -1143,6 +1198,17 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
         fx_sh += fx_store_normalise(w, fx_slots() + 32 * ((NS8 + 1) & 1));
         sdf = fx_e == INT_MIN ? INT_MIN : fx_e + fx_sh;
         if (tid < L && g0 + tid < a.nlines) a.lexp_out[a.gout_off + g0 + tid] = sdf == INT_MIN ? INT_MAX : sdf;
+      }
+    }
+    if constexpr (IO != 0 && is_fx<P>()) {
+      if (a.pair && (a.mode == 1 || a.mode == 3)) {  // r2c / REDFT10: separate the two spectra
+        int pos[8];
+#pragma unroll
+        for (int b = 0; b < NB; b++)
+#pragma unroll
+          for (int r = 0; r < Q; r++) pos[b * Q + r] = t + b * TPL + r * NQ;
+        fx_pair_store<P, IO == 2, ROW_OUT, N, L, LSP>(a, w, pos, l, buf, offO, g0, sdf);
+        return;
       }
     }
     if (ROW_IN == ROW_OUT) {

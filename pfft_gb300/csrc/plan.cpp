@@ -96,6 +96,22 @@ static void mark_quant(const Plan* pl, PassProgram* prog) {
   for (Pass& ps : prog->passes) ps.p.quant = pl->quant;
 }
 
+// Default double plans: r2c and REDFT10 passes on the radix-8 kernel whose
+// batch dimension 0 has an even extent transform two real lines per complex
+// line (PassParams::pair; fast_args applies it).  A paired pass keeps double
+// output (no FX link out of it).
+static void mark_pair(const Plan* pl, PassProgram* prog) {
+  for (Pass& ps : prog->passes) {
+    PassParams& p = ps.p;
+    p.pair = 0;
+    if (pl->arith != ARITH_F64 || p.quant != 2) continue;
+    if (p.mode != MODE_R2C && p.mode != MODE_RE10) continue;
+    if (p.nb < 1 || p.bext[0] % 2) continue;
+    if (!fast_pass_eligible(p, pl->arith)) continue;
+    p.pair = 1;
+  }
+}
+
 // FX mantissas kept between two consecutive radix-8 passes of a default
 // double plan (PassParams::fx_out / fx_in): the first pass stores its int64
 // mantissas and one exponent per line, the second reads them and aligns each
@@ -139,7 +155,7 @@ static bool link_fx(Plan* pl, PassProgram* prog, std::vector<int*>* lexp) {
     PassParams& a = prog->passes[i].p;
     PassParams& b = prog->passes[i + 1].p;
     const bool b_plain = b.mode == MODE_C2C && b.Zi == 0 && b.Ni == b.N && b.Zo == 0 && b.No == b.N && !b.wmode;
-    if (!b_plain || (a.mode != MODE_C2C && a.mode != MODE_R2C)) continue;
+    if (!b_plain || (a.mode != MODE_C2C && a.mode != MODE_R2C) || a.pair) continue;
     if ((a.N & (a.N - 1)) || (b.N & (b.N - 1))) continue;  // the radix-8 kernel on both sides
     if (!fast_pass_eligible(a, pl->arith) || !fast_pass_eligible(b, pl->arith)) continue;
     // b's input dimensions onto a's output dimensions.  Both passes' planner
@@ -296,6 +312,7 @@ Plan* make_plan(const PlanDesc& base, void* in, void* out) {
     return nullptr;
   }
   mark_quant(pl, &pl->fwd);
+  mark_pair(pl, &pl->fwd);
   if (!ensure_workspace(pl, pl->fwd)) {
     destroy_plan(pl);
     return nullptr;
@@ -555,6 +572,7 @@ void execute_plan(Plan* pl, void* in, void* out, bool adjoint) {
       return;
     }
     mark_quant(pl, &pl->adj);
+    mark_pair(pl, &pl->adj);
     if (!ensure_workspace(pl, pl->adj)) return;
     apply_wisdom(&pl->adj, pl->arith);
     if ((pl->d.pfft_flags & (F_PATIENT | F_EXHAUSTIVE | F_TUNE)) && !tune_program(pl, &pl->adj)) return;

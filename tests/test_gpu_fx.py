@@ -10,11 +10,13 @@ layout, exactly invariant under power-of-two scaling of the input (the grid
 follows the exponent), and must turn a tile holding an infinity or NaN into
 NaN instead of garbage.
 """
+import ctypes
+
 import numpy as np
 import pytest
 
 import pfft_gb300 as pg
-from tests.pfft_util import Req, gpu_run, oracle_run, random_input, rel_l2
+from tests.pfft_util import Req, gpu_run, mask_padding, oracle_run, random_input, rel_l2
 
 pytestmark = pytest.mark.gpu
 
@@ -191,3 +193,52 @@ def test_fx_links_form(cuda, pfft_lib, n, flags, links):
         assert got[1] == 0
     else:
         assert got == links
+
+
+@pytest.mark.parametrize("kind,n,flags,kinds", [
+    ("r2c", (8, 16, 32), 0, None),                                          # paired (128 rows)
+    ("r2c", (32, 32, 64), pg.PFFT_PADDED_R2C | pg.PFFT_TRANSPOSED_OUT, None),  # the benchmark's layout
+    ("r2c", (3, 5, 64), 0, None),                                           # 15 rows: not paired
+    ("r2c", (4, 6, 4096), 0, None),                                         # one-line tiles
+    ("r2r", (16, 32, 64), 0, [5, 5, 5]),                                    # REDFT10 on every axis
+    ("r2r", (6, 8, 256), 0, [5, 5, 5]),
+    ("c2r", (32, 32, 64), pg.PFFT_PADDED_R2C | pg.PFFT_TRANSPOSED_IN, None),  # inverse kinds: not paired
+    ("r2r", (16, 32, 64), 0, [4, 4, 4]),                                    # REDFT01
+])
+def test_fx_paired_real_lines(cuda, pfft_lib, kind, n, flags, kinds):
+    """r2c and REDFT10 passes of default double plans transform two real
+    lines (adjacent along the pass's first batch dimension, when its extent
+    is even) as one complex line and separate the spectra afterwards; c2r and
+    REDFT01 passes do not pair.  Against
+    the oracle they stay within 1e-15 and within 1.25x native FP64's error,
+    and the plan reports the pairing (bit 2 of pfft_gb300_pass_fx_link)."""
+    sign = 1 if kind == "c2r" else -1
+    req = Req(kind, n, flags=flags, kinds=kinds) if kinds else Req(kind, n, flags=flags, sign=sign)
+    rng = np.random.default_rng(sum(n) + flags)
+    x = random_input(req, rng)
+    ref = mask_padding(req, oracle_run(req, x))  # (a padded real output's padding is undefined)
+    fx = mask_padding(req, gpu_run(req, x, prec="double"))
+    nat = mask_padding(req, gpu_run(req, x, prec="double-f64"))
+    e_fx, e_nat = rel_l2(fx, ref), rel_l2(nat, ref)
+    assert e_fx <= 1e-15, e_fx
+    assert e_fx <= 1.25 * e_nat + 1e-17, (e_fx, e_nat)
+    # which passes pair
+    torch = cuda
+    L = pfft_lib
+    cnt = int(np.prod(n))
+    a = torch.zeros(2 * cnt + 64 * n[0] * n[1], dtype=torch.float64, device="cuda")
+    b = torch.zeros_like(a)
+    if kind == "r2c":
+        p = L.pfft_plan_dft_r2c_3d(pg.ints(n), a.data_ptr(), b.data_ptr(), pg.procmesh(2), pg.PFFT_FORWARD, flags)
+    elif kind == "c2r":
+        p = L.pfft_plan_dft_c2r_3d(pg.ints(n), a.data_ptr(), b.data_ptr(), pg.procmesh(2), pg.PFFT_BACKWARD, flags)
+    else:
+        p = L.pfft_plan_r2r_3d(pg.ints(n), a.data_ptr(), b.data_ptr(), pg.procmesh(2), (ctypes.c_int * 3)(*kinds), flags)
+    assert p, pg.last_error()
+    vals = [L.pfft_gb300_pass_fx_link(p, i) for i in range(8)]  # -1 past the last pass
+    L.pfft_destroy_plan(p)
+    paired = sum(1 for v in vals if v >= 0 and v & 4)
+    if n == (3, 5, 64) or kind == "c2r" or kinds == [4, 4, 4]:
+        assert paired == 0  # odd batch extent; the inverse kinds do not pair
+    else:
+        assert paired >= 1, vals
