@@ -211,7 +211,7 @@ bool fast_args(const PassParams& p, int arith, FastArgs* a, bool* row_in, bool* 
   // paired real lines: batch dimension 0 halved, its odd lines the partners
   a->pair = 0;
   if (p.pair && arith == ARITH_F64 && !p.fx_in && !p.fx_out && p.nb >= 1 && p.bext[0] % 2 == 0 &&
-      (p.mode == MODE_R2C || p.mode == MODE_RE10)) {
+      (p.mode == MODE_R2C || p.mode == MODE_C2R || p.mode == MODE_RE10 || p.mode == MODE_RE01)) {
     a->pair = 1;
     a->pairI = p.bsI[0];
     a->pairO = p.bsO[0];
@@ -267,6 +267,8 @@ int launch_fast_pass(const PassParams& p, int arith, cudaStream_t stream) {
   a.staged = p.staged;
   // the FFT direction: the pass's, except for the DCTs (10 forward, 01 inverse)
   const int sign = a.mode == 3 ? -1 : (a.mode == 4 ? 1 : p.sign);
+  if (a.mode == 4 && arith == ARITH_F64 && a.pair)  // paired REDFT01
+    return sign > 0 ? launch_dct_pinv<FX, 1>(N, a, row_in, row_out, stream) : -1;
   if (a.mode >= 3 && arith == ARITH_F64)
     return sign < 0 ? launch_dct<FX, -1>(N, a, row_in, row_out, stream) : launch_dct<FX, 1>(N, a, row_in, row_out, stream);
   if (a.mode >= 3)
@@ -297,6 +299,9 @@ int launch_fast_pass(const PassParams& p, int arith, cudaStream_t stream) {
                                : launch_mixed_five<FDD, 1>(N, a, row_in, row_out, stream));
   }
   if (!a.plain) {  // r2c / c2r / windows / weights: the general-I/O instantiations
+    if (arith == ARITH_F64 && a.pair && a.mode == 2)  // paired c2r
+      return sign < 0 ? launch_gio_pinv<FX, -1>(N, a, row_in, row_out, stream)
+                      : launch_gio_pinv<FX, 1>(N, a, row_in, row_out, stream);
     if (arith == ARITH_F64)
       return sign < 0 ? launch_gio<FX, -1>(N, a, row_in, row_out, stream) : launch_gio<FX, 1>(N, a, row_in, row_out, stream);
     return arith == ARITH_F32 ? (sign < 0 ? launch_gio<F32, -1>(N, a, row_in, row_out, stream)

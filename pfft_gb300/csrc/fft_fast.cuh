@@ -721,6 +721,14 @@ struct FastArgs {
   long long pairI, pairO;
 };
 
+// IO kinds of the radix-8 kernel: 0 plain c2c lines, 1 general I/O (r2c,
+// c2r, windows, adjoint weights), 2 the DCTs; 3 and 4 the same as 1 and 2
+// for paired inverse passes (c2r, REDFT01: two real lines combined before
+// the transform, FX only), compiled separately so that the other kernels
+// carry none of their registers
+__host__ __device__ constexpr bool io_dct(int IO) { return IO == 2 || IO == 4; }
+__host__ __device__ constexpr bool io_pinv(int IO) { return IO >= 3; }
+
 // global element access: native format, or float-float pairs for the
 // intermediate arrays of the double API (same 16 bytes per complex value).
 // CG: load through L2 only (data written earlier in the same launch).
@@ -869,7 +877,7 @@ __device__ __forceinline__ typename P::C rx(const FastArgs& a, long long off, in
 // element e (0..N-1) of a line's logical input sequence (FastArgs comment);
 // DCT: the kernel runs a REDFT10 / REDFT01 pass (compiled separately, so the
 // other kernels carry no DCT code)
-template <class P, bool CG, bool DCT = false>
+template <class P, bool CG, bool DCT = false, bool PINV = false>
 __device__ __forceinline__ typename P::C load_elem(const FastArgs& a, long long off, int e, int N) {
   typedef typename P::C C;
   if constexpr (is_fx<P>()) {
@@ -903,6 +911,12 @@ __device__ __forceinline__ typename P::C load_elem(const FastArgs& a, long long 
   if constexpr (is_fx<P>()) {  // raw doubles until fx_enter
     if (a.conj_in) v = fx_conj_raw(v);
     if (a.wmode == 1 && k != 0 && 2 * k != N) v = fx_half_raw(v);
+    // paired c2r: the DC and Nyquist bins' imaginary parts (which a c2r
+    // ignores) zeroed, so that each line's spectrum is exactly Hermitian and
+    // its inverse real: nothing leaks into the partner line
+    if constexpr (PINV) {
+      if (k == 0 || 2 * k == N) v.y = 0;
+    }
     return mirror ? fx_conj_raw(v) : v;
   } else {
     if (a.conj_in) v = P::conj(v);
@@ -913,7 +927,7 @@ __device__ __forceinline__ typename P::C load_elem(const FastArgs& a, long long 
 
 // store logical output position e of a line (kept when Zo <= e < Zo + No)
 // (eo: FX's result exponent)
-template <class P, bool DCT = false>
+template <class P, bool DCT = false, bool PINV = false>
 __device__ __forceinline__ void store_elem(const FastArgs& a, long long off, int e, typename P::C v, int N,
                                            int eo = 0) {
   if constexpr (DCT) {
@@ -929,6 +943,11 @@ __device__ __forceinline__ void store_elem(const FastArgs& a, long long off, int
   if (k < 0 || k >= a.No) return;
   if (a.wmode == 2 && e != 0 && 2 * e != N) v = P::add(v, v);
   if (a.conj_out) v = P::conj(v);
+  if constexpr (PINV) {  // paired c2r / REDFT01: z = y_a + i y_b
+    rstore<P>(a.dst, off + (long long)k * a.sOa, v, eo);
+    rstore<P>(a.dst, off + a.pairO + (long long)k * a.sOa, {v.y, v.x}, eo);
+    return;
+  }
   if (a.mode >= 2)
     rstore<P>(a.dst, off + (long long)k * a.sOa, v, eo);
   else
@@ -990,7 +1009,7 @@ __host__ __device__ constexpr int fast_hdr(int L) {
 // shared memory (fast_smem_bytes).
 template <class P, int SIGN, int N, int L, bool ROW_IN, bool ROW_OUT, int IO>
 __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[8], long long g0, const long long* offO,
-                                          typename P::S* buf);
+                                          typename P::S* buf, const typename P::C* v2 = nullptr);
 // IO: 0 plain c2c lines (the hot kernels carry no other load/store code),
 // 1 r2c / c2r / windows / adjoint weights (load_elem, store_elem), 2 the DCTs
 template <class P, int SIGN, int N, int L, bool ROW_IN, bool ROW_OUT, bool CG = false, int IO = 0>
@@ -1046,9 +1065,16 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsi
     }
   } else {
 #pragma unroll
-    for (int r = 0; r < 8; r++) v[r] = load_elem<P, CG, IO == 2>(a, offI[l], t + r * TPL, N);
+    for (int r = 0; r < 8; r++) v[r] = load_elem<P, CG, io_dct(IO), io_pinv(IO)>(a, offI[l], t + r * TPL, N);
   }
-  fast_body<P, SIGN, N, L, ROW_IN, ROW_OUT, IO>(a, v, g0, offO, buf);
+  if constexpr (io_pinv(IO)) {  // paired c2r / REDFT01: line b's input beside line a's
+    C v2[8];
+#pragma unroll
+    for (int r = 0; r < 8; r++) v2[r] = load_elem<P, CG, io_dct(IO), true>(a, offI[l] + a.pairI, t + r * TPL, N);
+    fast_body<P, SIGN, N, L, ROW_IN, ROW_OUT, IO>(a, v, g0, offO, buf, v2);
+  } else {
+    fast_body<P, SIGN, N, L, ROW_IN, ROW_OUT, IO>(a, v, g0, offO, buf);
+  }
 }
 
 // Stages and store of one tile after the load: v holds elements t + r*TPL of
@@ -1056,7 +1082,7 @@ __device__ __forceinline__ void fast_tile(const FastArgs& a, long long blk, unsi
 // lines; buf the exchange area (L lines of lsp_of elements).
 template <class P, int SIGN, int N, int L, bool ROW_IN, bool ROW_OUT, int IO>
 __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[8], long long g0, const long long* offO,
-                                          typename P::S* buf) {
+                                          typename P::S* buf, const typename P::C* v2) {
   typedef typename P::C C;
   typedef typename P::S S;
   typedef typename P::G G;
@@ -1073,7 +1099,28 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
   S* line = buf + l * LSP;
   int sdf = a.out_df;  // FX: the results' exponent instead
   int fx_e = 0, fx_sh = 0;  // FX: the tile's grid exponent and the stages' shifts
-  if constexpr (is_fx<P>()) {
+  if constexpr (is_fx<P>() && io_pinv(IO)) {
+    // paired c2r / REDFT01: both lines on one grid, then z = X_a + i X_b
+    // (REDFT01: each line's spectrum rotated first), exact integer sums
+    C w[16];
+#pragma unroll
+    for (int r = 0; r < 8; r++) {
+      w[r] = v[r];
+      w[8 + r] = v2[r];
+    }
+    fx_e = fx_enter<N, 16>(w, 0);
+    if (a.mode == 4) {
+#pragma unroll
+      for (int r = 0; r < 8; r++) {
+        const typename P::W tw4 = P::template twd<1>(P::ldw(a.tw2, t + r * TPL, 4 * N));
+        w[r] = P::mul(w[r], tw4);
+        w[8 + r] = P::mul(w[8 + r], tw4);
+      }
+      fx_sh += 2;
+    }
+#pragma unroll
+    for (int r = 0; r < 8; r++) v[r] = {w[r].x - w[8 + r].y, w[r].y + w[8 + r].x};
+  } else if constexpr (is_fx<P>()) {
     if (IO == 0 && a.fx_in) {  // mantissas of the previous radix-8 pass, each with its line's exponent
       const long long gl = offO[L + l];
       int ex[8];
@@ -1083,7 +1130,7 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
     } else {
       fx_e = fx_enter<N>(v, IO == 0 ? a.conj_in : 0);  // IO 1: conjugated in load_elem
     }
-    if constexpr (IO == 2) {
+    if constexpr (io_dct(IO)) {
       if (a.mode == 4) {  // REDFT01: (x_k - i x_(N-k)) W_4N^-k, twiddles carrying 1/4
 #pragma unroll
         for (int r = 0; r < 8; r++) v[r] = P::mul(v[r], P::template twd<1>(P::ldw(a.tw2, t + r * TPL, 4 * N)));
@@ -1126,12 +1173,12 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
   }
   if (Q == 1) {
     // v holds the last stage (Ns = N/8, k = t): outputs y[t + r*TPL]
-    if constexpr (IO != 0 && is_fx<P>()) {
+    if constexpr ((IO == 1 || IO == 2) && is_fx<P>()) {
       if (a.pair && (a.mode == 1 || a.mode == 3)) {  // r2c / REDFT10: separate the two spectra
         int pos[8];
 #pragma unroll
         for (int r = 0; r < 8; r++) pos[r] = t + r * TPL;
-        fx_pair_store<P, IO == 2, ROW_OUT, N, L, LSP>(a, v, pos, l, buf, offO, g0, sdf);
+        fx_pair_store<P, io_dct(IO), ROW_OUT, N, L, LSP>(a, v, pos, l, buf, offO, g0, sdf);
         return;
       }
     }
@@ -1144,7 +1191,7 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
           for (int r = 0; r < 8; r++) gput<P>(a, dst + r * st, a.conj_out ? P::conj(v[r]) : v[r], sdf);
         } else {
 #pragma unroll
-          for (int r = 0; r < 8; r++) store_elem<P, IO == 2>(a, offO[l], t + r * TPL, v[r], N, sdf);
+          for (int r = 0; r < 8; r++) store_elem<P, io_dct(IO), io_pinv(IO)>(a, offO[l], t + r * TPL, v[r], N, sdf);
         }
       }
       return;
@@ -1200,14 +1247,14 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
         if (tid < L && g0 + tid < a.nlines) a.lexp_out[a.gout_off + g0 + tid] = sdf == INT_MIN ? INT_MAX : sdf;
       }
     }
-    if constexpr (IO != 0 && is_fx<P>()) {
+    if constexpr ((IO == 1 || IO == 2) && is_fx<P>()) {
       if (a.pair && (a.mode == 1 || a.mode == 3)) {  // r2c / REDFT10: separate the two spectra
         int pos[8];
 #pragma unroll
         for (int b = 0; b < NB; b++)
 #pragma unroll
           for (int r = 0; r < Q; r++) pos[b * Q + r] = t + b * TPL + r * NQ;
-        fx_pair_store<P, IO == 2, ROW_OUT, N, L, LSP>(a, w, pos, l, buf, offO, g0, sdf);
+        fx_pair_store<P, io_dct(IO), ROW_OUT, N, L, LSP>(a, w, pos, l, buf, offO, g0, sdf);
         return;
       }
     }
@@ -1226,7 +1273,7 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
 #pragma unroll
           for (int b = 0; b < NB; b++)
 #pragma unroll
-            for (int r = 0; r < Q; r++) store_elem<P, IO == 2>(a, offO[l], t + b * TPL + r * NQ, w[b * Q + r], N, sdf);
+            for (int r = 0; r < Q; r++) store_elem<P, io_dct(IO), io_pinv(IO)>(a, offO[l], t + b * TPL + r * NQ, w[b * Q + r], N, sdf);
         }
       }
       return;
@@ -1253,7 +1300,7 @@ __device__ __forceinline__ void fast_body(const FastArgs& a, typename P::C (&v)[
           if (a.conj_out) o = P::conj(o);
           gput<P>(a, d2 + (long long)k * a.sOa, o, sdf);
         } else {
-          store_elem<P, IO == 2>(a, offO[l2], k, o, N, sdf);
+          store_elem<P, io_dct(IO), io_pinv(IO)>(a, offO[l2], k, o, N, sdf);
         }
       }
     }
@@ -1488,6 +1535,12 @@ int launch_gio(int N, const FastArgs& a, bool row_in, bool row_out, cudaStream_t
 // orientation on both sides, default tile heights (fft_fast_dct_<arith>_<dir>.cu)
 template <class P, int SIGN>
 int launch_dct(int N, const FastArgs& a, bool row_in, bool row_out, cudaStream_t s);
+// paired inverse passes (IO kinds 3 and 4): c2r (fft_fast_gioinv_fx_<dir>.cu)
+// and REDFT01 (fft_fast_dctinv_fx_bwd.cu), 64-bit fixed point
+template <class P, int SIGN>
+int launch_gio_pinv(int N, const FastArgs& a, bool row_in, bool row_out, cudaStream_t s);
+template <class P, int SIGN>
+int launch_dct_pinv(int N, const FastArgs& a, bool row_in, bool row_out, cudaStream_t s);
 
 }  // namespace fast
 }  // namespace pg

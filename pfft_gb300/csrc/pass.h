@@ -135,11 +135,12 @@ struct PassParams {
                 // words (1) instead of TwoSum additions (0); double plans
                 // (ARITH_F64): 2 = the radix-8 kernel's 64-bit fixed-point
                 // arithmetic (fft_fast.cuh, FX) on the power-of-two passes
-  // FX r2c and REDFT10 passes: two real lines (adjacent along batch
-  // dimension 0, whose extent is even) transformed as the real and
-  // imaginary parts of one complex line, their spectra separated after the
-  // transform (host-set when the pass qualifies; fast_args halves batch
-  // dimension 0)
+  // FX r2c, c2r, REDFT10 and REDFT01 passes: two real lines (adjacent along
+  // batch dimension 0, whose extent is even) transformed as the real and
+  // imaginary parts of one complex line; the forward kinds separate the
+  // spectra after the transform, the inverse kinds (kernels of their own)
+  // combine them before it (host-set when the pass qualifies; fast_args
+  // halves batch dimension 0)
   int pair;
 };
 

@@ -96,16 +96,21 @@ static void mark_quant(const Plan* pl, PassProgram* prog) {
   for (Pass& ps : prog->passes) ps.p.quant = pl->quant;
 }
 
-// Default double plans: r2c and REDFT10 passes on the radix-8 kernel whose
-// batch dimension 0 has an even extent transform two real lines per complex
-// line (PassParams::pair; fast_args applies it).  A paired pass keeps double
-// output (no FX link out of it).
+// Default double plans: r2c, c2r, REDFT10 and REDFT01 passes on the radix-8
+// kernel whose batch dimension 0 has an even extent transform two real lines
+// per complex line (PassParams::pair; fast_args applies it).  A paired pass
+// keeps double output (no FX link out of it).
+static int g_pair = -1;  // PFFT_GB300_PAIR=0 turns the pairing off (comparisons)
 static void mark_pair(const Plan* pl, PassProgram* prog) {
+  if (g_pair < 0) {
+    const char* e = getenv("PFFT_GB300_PAIR");
+    g_pair = (e && strcmp(e, "0") == 0) ? 0 : 1;
+  }
   for (Pass& ps : prog->passes) {
     PassParams& p = ps.p;
     p.pair = 0;
-    if (pl->arith != ARITH_F64 || p.quant != 2) continue;
-    if (p.mode != MODE_R2C && p.mode != MODE_RE10) continue;
+    if (!g_pair || pl->arith != ARITH_F64 || p.quant != 2) continue;
+    if (p.mode != MODE_R2C && p.mode != MODE_C2R && p.mode != MODE_RE10 && p.mode != MODE_RE01) continue;
     if (p.nb < 1 || p.bext[0] % 2) continue;
     if (!fast_pass_eligible(p, pl->arith)) continue;
     p.pair = 1;
