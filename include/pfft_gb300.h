@@ -142,7 +142,11 @@ int pfft_gb300_get_double_arith(void);
 /* Mode 2 keeps the int64 mantissas (and one exponent per line) between two
  * consecutive radix-8 passes instead of rounding them to double in between
  * (on by default; the environment variable PFFT_GB300_FX_LINK=0 sets it off).
- * Applies to plans created afterwards.  Returns the previous setting. */
+ * Applies to plans created afterwards.  Returns the previous setting.
+ * Mode 2 also transforms two real lines per complex line in r2c, c2r,
+ * REDFT10 and REDFT01 passes whose first batch dimension has an even extent
+ * (pfft_gb300_pass_fx_link reports it); the environment variable
+ * PFFT_GB300_PAIR=0 turns that off for the process. */
 int pfft_gb300_set_fx_link(int on);
 
 /* Autotuning and wisdom.  Plans created with PFFT_PATIENT, PFFT_EXHAUSTIVE
