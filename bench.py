@@ -505,32 +505,37 @@ def measure_halo(L, pg, torch, peak, n=(256, 256, 256), w=2, reps=10):
     return res
 
 
-def measure_configs(L, pg, torch, peak):
-    """Every configuration of the metric besides the 512^3 headline (each a
+def config_table(pg):
+    """name -> (measure_config arguments after L, pg, torch; keyword arguments)
+    for every configuration of the metric besides the 512^3 headline (each a
     forward execute with the default arithmetic; algorithmic bytes
     B = in + out + 2 (P_min - 1) work)."""
     TO, TI, PAD = pg.PFFT_TRANSPOSED_OUT, pg.PFFT_TRANSPOSED_IN, pg.PFFT_PADDED_R2C
-    c = {}
-    c["c2c_64cube_c128"] = measure_config(L, pg, torch, "c2c", (64, 64, 64), "double", 0, 0,
-                                          2 * 2 * 64 ** 3 * 16, peak)
+    t = {"c2c_64cube_c128": (("c2c", (64, 64, 64), "double", 0, 0, 2 * 2 * 64 ** 3 * 16), {})}
     n256 = (256, 256, 256)
     for prec, esz in (("double", 8), ("float", 4)):
         tag = "f64" if prec == "double" else "f32"
         rin = 256 * 256 * 258 * esz
         cout = 256 * 256 * 129 * 2 * esz
-        c["r2c_256cube_%s_padded_transposed_inplace" % tag] = measure_config(
-            L, pg, torch, "r2c", n256, prec, PAD | TO, PAD | TI, rin + cout + 2 * cout, peak, inplace=True,
-            dist="normal")
+        t["r2c_256cube_%s_padded_transposed_inplace" % tag] = (
+            ("r2c", n256, prec, PAD | TO, PAD | TI, rin + cout + 2 * cout), {"inplace": True, "dist": "normal"})
         rb = 256 ** 3 * esz
-        c["redft10_256cube_%s" % tag] = measure_config(
-            L, pg, torch, "r2r", n256, prec, 0, 0, 4 * rb, peak, kinds=[pg.PFFT_REDFT10] * 3,
-            kinds_inv=[pg.PFFT_REDFT01] * 3, norm=float((2 * 256) ** 3), dist="normal")
-    c["ousam_r2c_f32_128to256"] = measure_config(L, pg, torch, "r2c", n256, "float", 0, 0, 211 * 10 ** 6, peak,
-                                                 ni=(128, 128, 128), dist="normal")
-    c["c2c_1024cube_c64"] = measure_config(L, pg, torch, "c2c", (1024, 1024, 1024), "float", 0, 0,
-                                           3 * 2 * 1024 ** 3 * 8, peak, reps=5)
-    c["c2c_64pow4_c128"] = measure_config(L, pg, torch, "c2c", (64, 64, 64, 64), "double", 0, 0,
-                                          2 * 2 * 64 ** 4 * 16, peak)
+        t["redft10_256cube_%s" % tag] = (
+            ("r2r", n256, prec, 0, 0, 4 * rb),
+            {"kinds": [pg.PFFT_REDFT10] * 3, "kinds_inv": [pg.PFFT_REDFT01] * 3, "norm": float((2 * 256) ** 3),
+             "dist": "normal"})
+    t["ousam_r2c_f32_128to256"] = (("r2c", n256, "float", 0, 0, 211 * 10 ** 6),
+                                   {"ni": (128, 128, 128), "dist": "normal"})
+    t["c2c_1024cube_c64"] = (("c2c", (1024, 1024, 1024), "float", 0, 0, 3 * 2 * 1024 ** 3 * 8), {"reps": 5})
+    t["c2c_64pow4_c128"] = (("c2c", (64, 64, 64, 64), "double", 0, 0, 2 * 2 * 64 ** 4 * 16), {})
+    return t
+
+
+def measure_configs(L, pg, torch, peak):
+    """Every configuration of config_table, then the 256^3 halo."""
+    c = {}
+    for name, (args, kw) in config_table(pg).items():
+        c[name] = measure_config(L, pg, torch, *args, peak, **kw)
     c["halo_256cube_w2_f64"] = measure_halo(L, pg, torch, peak)
     return c
 
@@ -626,6 +631,8 @@ def main():
                     help="print only the batched-vs-loop measurement of that precision (profiling runs)")
     ap.add_argument("--halo-only", action="store_true",
                     help="print only the 256^3 halo exchange / reduce measurement (profiling runs)")
+    ap.add_argument("--config-only", default=None,
+                    help="print only the measurement of one named configuration (profiling runs)")
     ap.add_argument("--prec", default="double", choices=["double", "float"],
                     help="double = pfft_ (complex128, the headline); float = pfftf_ (complex64)")
     args = ap.parse_args()
@@ -644,6 +651,10 @@ def main():
         return
     if args.halo_only:
         print(json.dumps(measure_halo(L, pg, torch, measured_peak())), flush=True)
+        return
+    if args.config_only:
+        cargs, kw = config_table(pg)[args.config_only]
+        print(json.dumps(measure_config(L, pg, torch, *cargs, measured_peak(), **kw)), flush=True)
         return
     dev = torch.device("cuda", local)
     n = tuple(int(v) for v in args.shape.split("x")) if args.shape else (args.n, args.n, args.n)
